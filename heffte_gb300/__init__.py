@@ -1,0 +1,329 @@
+"""heffte_gb300 — Python host side of the GB300-native fft3d backend.
+
+ctypes over the C ABI of ``libheffte_gb300.so`` (declared in
+``include/heffte_gb300.h``), mirroring the reference's own Python binding
+(python/heffte.py:116-462: ``box3d``, ``scale``, ``fft3d``, ``fft3d_r2c``,
+``forward``/``backward`` and their ``_buffered`` variants, ``size_*``) for one
+rank.  Arrays are CUDA tensors (torch is only the device-memory container);
+raw device pointers (ints) are accepted by the ``*_ptr`` methods.
+
+There is no CPU fallback: importing the package raises if the library is not
+built (``python -m heffte_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+__all__ = ["box3d", "scale", "kind", "plan_options", "fft3d", "fft3d_r2c", "rtransform", "executor",
+           "heffte_input_error", "HeffteError", "lib", "library_path"]
+
+
+class heffte_input_error(Exception):
+    """Invalid input detected on the host, as python/heffte.py:31-36."""
+
+
+class HeffteError(RuntimeError):
+    """A status code returned by the library (message as the reference's runtime_error)."""
+
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+library_path = _build.LIB
+_lib = None
+
+
+def lib():
+    """Loads libheffte_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(library_path):
+        raise ImportError("libheffte_gb300.so is not built: run `python -m heffte_gb300.build` "
+                          "(the package has no CPU fallback)")
+    L = ctypes.CDLL(library_path)
+    vp, i, ll, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+    I3 = ctypes.c_int * 3
+    LL3 = ctypes.c_longlong * 3
+    L.heffte_gb300_last_error.restype = ctypes.c_char_p
+    L.heffte_gb300_convert.argtypes = [vp, i, ll, vp, vp, i]
+    L.heffte_gb300_scale_data.argtypes = [vp, i, ll, vp, d]
+    L.heffte_gb300_direct_pack.argtypes = [vp, i, ll, ll, ll, ll, ll, vp, vp]
+    L.heffte_gb300_direct_unpack.argtypes = [vp, i, ll, ll, ll, ll, ll, vp, vp]
+    L.heffte_gb300_transpose_unpack.argtypes = [vp, i, ll, ll, ll, ll, ll, ll, ll, i, i, i, vp, vp]
+    L.heffte_gb300_executor_create.argtypes = [i, LL3, LL3, I3, i, I3, ctypes.POINTER(vp)]
+    L.heffte_gb300_executor_destroy.argtypes = [vp]
+    for f in ("box_size", "complex_size", "workspace_size"):
+        getattr(L, "heffte_gb300_executor_" + f).argtypes = [vp]
+        getattr(L, "heffte_gb300_executor_" + f).restype = ll
+    L.heffte_gb300_executor_forward.argtypes = [vp, vp, i, vp, vp, vp]
+    L.heffte_gb300_executor_backward.argtypes = [vp, vp, i, vp, vp, vp]
+    L.heffte_gb300_set_default_options.argtypes = [ctypes.c_void_p]
+    L.heffte_gb300_plan_create.argtypes = [i, I3, I3, I3, I3, I3, I3, i, vp, vp, ctypes.POINTER(vp)]
+    L.heffte_gb300_plan_destroy.argtypes = [vp]
+    L.heffte_gb300_plan_set_stream.argtypes = [vp, vp]
+    for f in ("size_inbox", "size_outbox", "size_workspace"):
+        getattr(L, "heffte_gb300_" + f).argtypes = [vp]
+        getattr(L, "heffte_gb300_" + f).restype = ll
+    L.heffte_gb300_scale_factor.argtypes = [vp, i]
+    L.heffte_gb300_scale_factor.restype = d
+    L.heffte_gb300_forward.argtypes = [vp, i, vp, vp, vp, i]
+    L.heffte_gb300_backward.argtypes = [vp, i, vp, vp, vp, i]
+    L.heffte_gb300_forward_batch.argtypes = [vp, i, i, vp, vp, vp, i]
+    L.heffte_gb300_backward_batch.argtypes = [vp, i, i, vp, vp, vp, i]
+    _lib = L
+    return L
+
+
+def check(code):
+    if code != 0:
+        msg = lib().heffte_gb300_last_error().decode()
+        raise HeffteError(code, msg or f"heffte_gb300 error {code}")
+
+
+class scale:
+    """heffte::scale (include/heffte_fft3d.h:140-147)."""
+    none = 0
+    full = 1
+    symmetric = 2
+
+
+class kind:
+    c2c = 0
+    r2c = 1
+    cos = 2
+    sin = 3
+
+
+class box3d:
+    """box3d (include/heffte_geometry.h:67-133): inclusive low/high, order o0 fastest."""
+
+    def __init__(self, clow, chigh, corder=(0, 1, 2)):
+        self.low = tuple(int(v) for v in clow)
+        self.high = tuple(int(v) for v in chigh)
+        self.order = tuple(int(v) for v in corder)
+        if len(self.low) != 3 or len(self.high) != 3 or sorted(self.order) != [0, 1, 2]:
+            raise heffte_input_error("box3d needs three low, three high indexes and an order permutation")
+        self.size = tuple(self.high[i] - self.low[i] + 1 for i in range(3))
+
+    def count(self):
+        return 0 if min(self.size) <= 0 else self.size[0] * self.size[1] * self.size[2]
+
+    def r2c(self, dimension):
+        hi = list(self.high)
+        hi[dimension] = self.low[dimension] + self.size[dimension] // 2
+        return box3d(self.low, hi, self.order)
+
+    def osize(self, d):
+        return self.size[self.order[d]]
+
+    def __repr__(self):
+        return f"box3d({self.low}, {self.high}, {self.order})"
+
+
+class plan_options(ctypes.Structure):
+    """plan_options (include/heffte_plan_logic.h:131-176), C layout of heffte_plan_options."""
+    _fields_ = [("use_reorder", ctypes.c_int), ("algorithm", ctypes.c_int),
+                ("use_pencils", ctypes.c_int), ("use_gpu_aware", ctypes.c_int)]
+
+    @staticmethod
+    def default():
+        o = plan_options()
+        check(lib().heffte_gb300_set_default_options(ctypes.byref(o)))
+        return o
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)  # torch.cuda.Stream
+
+
+def _ptr(x):
+    if isinstance(x, int):
+        return x
+    if x is None:
+        return None
+    if not x.is_cuda:
+        raise heffte_input_error("arrays must live on the GPU (no CPU fallback)")
+    if not x.is_contiguous():
+        raise heffte_input_error("arrays must be contiguous")
+    return x.data_ptr()
+
+
+_REAL = {"torch.float32": 0, "torch.float64": 1}
+_CPLX = {"torch.complex64": 0, "torch.complex128": 1}
+
+
+class _plan:
+    """A single-rank 3-D transform plan (fft3d / fft3d_r2c / rtransform)."""
+
+    def __init__(self, tkind, inbox, outbox, r2c_direction=0, options=None, stream=None):
+        L = lib()
+        self.kind = tkind
+        self.inbox, self.outbox = inbox, outbox
+        self._h = ctypes.c_void_p()
+        I3 = ctypes.c_int * 3
+        opts = options if options is not None else plan_options.default()
+        self.stream = _stream_handle(stream)
+        check(L.heffte_gb300_plan_create(tkind, I3(*inbox.low), I3(*inbox.high), I3(*inbox.order),
+                                         I3(*outbox.low), I3(*outbox.high), I3(*outbox.order),
+                                         r2c_direction, ctypes.byref(opts), self.stream, ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.heffte_gb300_plan_destroy(h)
+            self._h = None
+
+    def set_stream(self, stream):
+        self.stream = _stream_handle(stream)
+        check(lib().heffte_gb300_plan_set_stream(self._h, self.stream))
+
+    def size_inbox(self):
+        return lib().heffte_gb300_size_inbox(self._h)
+
+    def size_outbox(self):
+        return lib().heffte_gb300_size_outbox(self._h)
+
+    def size_workspace(self):
+        return lib().heffte_gb300_size_workspace(self._h)
+
+    def get_scale_factor(self, scaling):
+        return lib().heffte_gb300_scale_factor(self._h, scaling)
+
+    # -- type checks mirroring python/heffte.py:236-300 --
+    def _prec(self, inarray, outarray, forward):
+        it, ot = str(inarray.dtype), str(outarray.dtype)
+        if self.kind == kind.c2c:
+            if it not in _CPLX or it != ot:
+                raise heffte_input_error("c2c transforms need complex64 or complex128 arrays of the same type")
+            return _CPLX[it]
+        if self.kind == kind.r2c:
+            rt, ct = (it, ot) if forward else (ot, it)
+            if rt not in _REAL or ct not in _CPLX or _REAL[rt] != _CPLX[ct]:
+                raise heffte_input_error("r2c transforms need float32/complex64 or float64/complex128 pairs")
+            return _REAL[rt]
+        if it not in _REAL or it != ot:
+            raise heffte_input_error("real-to-real transforms need float32 or float64 arrays of the same type")
+        return _REAL[it]
+
+    def _run(self, forward, inarray, outarray, workspace, scaling, batch=1):
+        if scaling not in (0, 1, 2):
+            raise heffte_input_error("called with invalid scaling")
+        nin, nout = (self.size_inbox(), self.size_outbox()) if forward else (self.size_outbox(), self.size_inbox())
+        if inarray.numel() < batch * nin or outarray.numel() < batch * nout:
+            raise heffte_input_error("called with invalid array size")
+        prec = self._prec(inarray, outarray, forward)
+        L = lib()
+        f = L.heffte_gb300_forward_batch if forward else L.heffte_gb300_backward_batch
+        check(f(self._h, batch, prec, _ptr(inarray), _ptr(outarray), _ptr(workspace), scaling))
+
+    def forward(self, inarray, outarray, scaling=scale.none):
+        self._run(True, inarray, outarray, None, scaling)
+
+    def backward(self, inarray, outarray, scaling=scale.none):
+        self._run(False, inarray, outarray, None, scaling)
+
+    def forward_buffered(self, inarray, outarray, workspace, scaling=scale.none):
+        self._run(True, inarray, outarray, workspace, scaling)
+
+    def backward_buffered(self, inarray, outarray, workspace, scaling=scale.none):
+        self._run(False, inarray, outarray, workspace, scaling)
+
+    def forward_batch(self, batch, inarray, outarray, scaling=scale.none, workspace=None):
+        self._run(True, inarray, outarray, workspace, scaling, batch)
+
+    def backward_batch(self, batch, inarray, outarray, scaling=scale.none, workspace=None):
+        self._run(False, inarray, outarray, workspace, scaling, batch)
+
+    # raw-pointer entry points (prec 0 single / 1 double)
+    def forward_ptr(self, prec, inp, out, workspace=0, scaling=scale.none, batch=1):
+        check(lib().heffte_gb300_forward_batch(self._h, batch, prec, inp, out, workspace or None, scaling))
+
+    def backward_ptr(self, prec, inp, out, workspace=0, scaling=scale.none, batch=1):
+        check(lib().heffte_gb300_backward_batch(self._h, batch, prec, inp, out, workspace or None, scaling))
+
+
+def fft3d(inbox, outbox, options=None, stream=None):
+    """heffte::fft3d<backend::gb300> on one rank (include/heffte_fft3d.h:270-297)."""
+    return _plan(kind.c2c, inbox, outbox, 0, options, stream)
+
+
+def fft3d_r2c(inbox, outbox, r2c_direction, options=None, stream=None):
+    """heffte::fft3d_r2c<backend::gb300> on one rank (include/heffte_fft3d_r2c.h:76-93)."""
+    if r2c_direction not in (0, 1, 2):
+        raise heffte_input_error("fft3d_r2c() called with invalid r2c_direction, must use 0, 1, or 2")
+    return _plan(kind.r2c, inbox, outbox, r2c_direction, options, stream)
+
+
+def rtransform(rkind, inbox, outbox, options=None, stream=None):
+    """heffte::rtransform<backend::gb300_cos|gb300_sin> (include/heffte_fft3d.h:748-749)."""
+    if rkind not in (kind.cos, kind.sin):
+        raise heffte_input_error("rtransform kind must be kind.cos or kind.sin")
+    return _plan(rkind, inbox, outbox, 0, options, stream)
+
+
+class executor:
+    """one_dim_backend<gb300>::executor / executor_r2c on one box."""
+
+    def __init__(self, ekind, box, dims):
+        L = lib()
+        self._h = ctypes.c_void_p()
+        dims = list(dims)
+        d3 = (ctypes.c_int * 3)(*(dims + [0] * (3 - len(dims))))
+        check(L.heffte_gb300_executor_create(ekind, (ctypes.c_longlong * 3)(*box.low),
+                                             (ctypes.c_longlong * 3)(*box.high), (ctypes.c_int * 3)(*box.order),
+                                             len(dims), d3, ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.heffte_gb300_executor_destroy(h)
+
+    def box_size(self):
+        return lib().heffte_gb300_executor_box_size(self._h)
+
+    def complex_size(self):
+        return lib().heffte_gb300_executor_complex_size(self._h)
+
+    def workspace_size(self):
+        return lib().heffte_gb300_executor_workspace_size(self._h)
+
+    def forward(self, prec, inp, out, stream=None):
+        check(lib().heffte_gb300_executor_forward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out), None))
+
+    def backward(self, prec, inp, out, stream=None):
+        check(lib().heffte_gb300_executor_backward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out), None))
+
+
+# -- location layer ---------------------------------------------------------
+def direct_pack(dtype, nfast, nmid, nslow, line_stride, plane_stride, src, dst, stream=None):
+    check(lib().heffte_gb300_direct_pack(_stream_handle(stream), dtype, nfast, nmid, nslow, line_stride,
+                                         plane_stride, _ptr(src), _ptr(dst)))
+
+
+def direct_unpack(dtype, nfast, nmid, nslow, line_stride, plane_stride, src, dst, stream=None):
+    check(lib().heffte_gb300_direct_unpack(_stream_handle(stream), dtype, nfast, nmid, nslow, line_stride,
+                                           plane_stride, _ptr(src), _ptr(dst)))
+
+
+def transpose_unpack(dtype, nfast, nmid, nslow, line_stride, plane_stride, buff_line_stride, buff_plane_stride,
+                     mp, src, dst, stream=None):
+    check(lib().heffte_gb300_transpose_unpack(_stream_handle(stream), dtype, nfast, nmid, nslow, line_stride,
+                                              plane_stride, buff_line_stride, buff_plane_stride, mp[0], mp[1], mp[2],
+                                              _ptr(src), _ptr(dst)))
+
+
+def scale_data(prec, num_reals, data, factor, stream=None):
+    check(lib().heffte_gb300_scale_data(_stream_handle(stream), prec, num_reals, _ptr(data), factor))
+
+
+def convert(prec, n, src, dst, to_complex, stream=None):
+    check(lib().heffte_gb300_convert(_stream_handle(stream), prec, n, _ptr(src), _ptr(dst), int(to_complex)))

@@ -1,0 +1,243 @@
+// extern "C" boundary of libheffte_gb300 (declarations in include/heffte_gb300.h).
+#include "gbfft_plan.h"
+#include "../../include/heffte_gb300.h"
+#include <cstring>
+#include <new>
+
+using namespace gbfft;
+
+struct heffte_gb300_executor_s { std::unique_ptr<Executor> e; };
+struct heffte_gb300_plan_s { std::unique_ptr<Plan3D> p; };
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template<class F>
+int guard(F &&fn){
+    try {
+        fn();
+        g_last_error.clear();
+        return HEFFTE_GB300_SUCCESS;
+    } catch (Error const &e){
+        g_last_error = e.what();
+        return e.code;
+    } catch (std::bad_alloc const &){
+        g_last_error = "host allocation failed";
+        return HEFFTE_GB300_ALLOC_ERROR;
+    } catch (std::exception const &e){
+        g_last_error = e.what();
+        return HEFFTE_GB300_INVALID;
+    }
+}
+
+cudaStream_t as_stream(void *s){ return reinterpret_cast<cudaStream_t>(s); }
+
+void check_dtype(int dtype){
+    if (dtype < 0 || dtype > 3) throw Error(ST_INVALID, "unknown element type code " + std::to_string(dtype));
+}
+void check_prec(int prec){
+    if (prec != 0 && prec != 1) throw Error(ST_INVALID, "precision must be 0 (single) or 1 (double)");
+}
+void check_sizes(long long a, long long b, long long c){
+    if (a < 0 || b < 0 || c < 0) throw Error(ST_INVALID, "negative size");
+}
+
+std::array<int, 3> order_of(int const *o){
+    if (!o) return {0, 1, 2};
+    std::array<int, 3> r{o[0], o[1], o[2]};
+    if (!valid_order(r)) throw Error(ST_INVALID, "order must be a permutation of 0, 1, 2");
+    return r;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *heffte_gb300_last_error(void){ return g_last_error.c_str(); }
+int heffte_gb300_version(void){ return 10000; }
+
+int heffte_gb300_convert(void *stream, int prec, long long n, const void *src, void *dst, int to_complex){
+    return guard([&]{
+        check_prec(prec);
+        if (n < 0) throw Error(ST_INVALID, "negative size");
+        if (n == 0) return;
+        if (!src || !dst) throw Error(ST_INVALID, "null pointer");
+        launch_convert(as_stream(stream), prec, n, src, dst, to_complex != 0);
+        check_cuda(cudaPeekAtLastError(), "convert kernel launch");
+    });
+}
+
+int heffte_gb300_scale_data(void *stream, int prec, long long num_reals, void *data, double factor){
+    return guard([&]{
+        check_prec(prec);
+        if (num_reals < 0) throw Error(ST_INVALID, "negative size");
+        if (num_reals == 0) return;   // empty box is allowed (src/heffte_backend_cuda.cu:473)
+        if (!data) throw Error(ST_INVALID, "null pointer");
+        launch_scale(as_stream(stream), prec, num_reals, data, factor);
+        check_cuda(cudaPeekAtLastError(), "scale kernel launch");
+    });
+}
+
+static int pack_common(void *stream, int dtype, long long nf, long long nm, long long ns, long long ls, long long ps,
+                       const void *src, void *dst, bool pack){
+    return guard([&]{
+        check_dtype(dtype);
+        check_sizes(nf, nm, ns);
+        if (nf == 0 || nm == 0 || ns == 0) return;
+        if (!src || !dst) throw Error(ST_INVALID, "null pointer");
+        launch_direct_pack(as_stream(stream), dtype, nf, nm, ns, ls, ps, src, dst, pack);
+        check_cuda(cudaPeekAtLastError(), pack ? "direct_pack kernel launch" : "direct_unpack kernel launch");
+    });
+}
+
+int heffte_gb300_direct_pack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
+                             long long line_stride, long long plane_stride, const void *src, void *dst){
+    return pack_common(stream, dtype, nfast, nmid, nslow, line_stride, plane_stride, src, dst, true);
+}
+
+int heffte_gb300_direct_unpack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
+                               long long line_stride, long long plane_stride, const void *src, void *dst){
+    return pack_common(stream, dtype, nfast, nmid, nslow, line_stride, plane_stride, src, dst, false);
+}
+
+int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
+                                  long long line_stride, long long plane_stride,
+                                  long long buff_line_stride, long long buff_plane_stride,
+                                  int map0, int map1, int map2, const void *src, void *dst){
+    return guard([&]{
+        check_dtype(dtype);
+        check_sizes(nfast, nmid, nslow);
+        if (!valid_order({map0, map1, map2})) throw Error(ST_INVALID, "map must be a permutation of 0, 1, 2");
+        if (nfast == 0 || nmid == 0 || nslow == 0) return;
+        if (!src || !dst) throw Error(ST_INVALID, "null pointer");
+        launch_transpose_unpack(as_stream(stream), dtype, nfast, nmid, nslow, line_stride, plane_stride,
+                                buff_line_stride, buff_plane_stride, map0, map1, src, dst);
+        check_cuda(cudaPeekAtLastError(), "transpose_unpack kernel launch");
+    });
+}
+
+// ---------------------------------------------------------------------------
+int heffte_gb300_executor_create(int kind, const long long low[3], const long long high[3], const int order[3],
+                                 int ndims, const int dims[3], heffte_gb300_executor *out){
+    return guard([&]{
+        if (!out || !low || !high || !dims) throw Error(ST_INVALID, "null pointer");
+        *out = nullptr;
+        if (kind < 0 || kind > 3) throw Error(ST_INVALID, "unknown executor kind");
+        if (ndims < 1 || ndims > 3) throw Error(ST_INVALID, "ndims must be 1, 2 or 3");
+        Box3 box({low[0], low[1], low[2]}, {high[0], high[1], high[2]}, order_of(order));
+        std::vector<int> d(dims, dims + ndims);
+        auto e = make_executor(kind, box, d);
+        if (!e) return;
+        auto *h = new heffte_gb300_executor_s;
+        h->e = std::move(e);
+        *out = h;
+    });
+}
+
+int heffte_gb300_executor_destroy(heffte_gb300_executor e){
+    return guard([&]{ delete e; });
+}
+
+long long heffte_gb300_executor_box_size(heffte_gb300_executor e){ return e ? e->e->box_size() : 0; }
+long long heffte_gb300_executor_complex_size(heffte_gb300_executor e){ return e ? e->e->complex_size() : 0; }
+long long heffte_gb300_executor_workspace_size(heffte_gb300_executor e){ return e ? e->e->workspace_size() : 0; }
+
+int heffte_gb300_executor_forward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
+                                  void *workspace){
+    (void)workspace;
+    return guard([&]{
+        if (!e) throw Error(ST_INVALID, "null executor");
+        check_prec(prec);
+        if (!in || !out) throw Error(ST_INVALID, "null pointer");
+        e->e->forward(as_stream(stream), prec, in, out);
+    });
+}
+
+int heffte_gb300_executor_backward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
+                                   void *workspace){
+    (void)workspace;
+    return guard([&]{
+        if (!e) throw Error(ST_INVALID, "null executor");
+        check_prec(prec);
+        if (!in || !out) throw Error(ST_INVALID, "null pointer");
+        e->e->backward(as_stream(stream), prec, in, out);
+    });
+}
+
+// ---------------------------------------------------------------------------
+int heffte_gb300_set_default_options(heffte_gb300_plan_options *o){
+    return guard([&]{
+        if (!o) throw Error(ST_INVALID, "null options");
+        o->use_reorder = 0;
+        o->algorithm = 0;
+        o->use_pencils = 1;
+        o->use_gpu_aware = 1;
+    });
+}
+
+int heffte_gb300_plan_create(int kind, const int inbox_low[3], const int inbox_high[3], const int *inbox_order,
+                             const int outbox_low[3], const int outbox_high[3], const int *outbox_order,
+                             int r2c_direction, const heffte_gb300_plan_options *options, void *stream,
+                             heffte_gb300_plan *plan){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan pointer");
+        *plan = nullptr;
+        if (!inbox_low || !inbox_high || !outbox_low || !outbox_high) throw Error(ST_INVALID, "null box pointer");
+        if (kind < 0 || kind > 3) throw Error(ST_INVALID, "unknown transform kind");
+        Box3 ib({inbox_low[0], inbox_low[1], inbox_low[2]}, {inbox_high[0], inbox_high[1], inbox_high[2]},
+                order_of(inbox_order));
+        Box3 ob({outbox_low[0], outbox_low[1], outbox_low[2]}, {outbox_high[0], outbox_high[1], outbox_high[2]},
+                order_of(outbox_order));
+        Options o;
+        if (options){
+            o.use_reorder = options->use_reorder != 0;
+            o.algorithm = options->algorithm;
+            o.use_pencils = options->use_pencils != 0;
+            o.use_gpu_aware = options->use_gpu_aware != 0;
+        }
+        auto p = make_plan(kind, ib, ob, r2c_direction, o, as_stream(stream));
+        auto *h = new heffte_gb300_plan_s;
+        h->p = std::move(p);
+        *plan = h;
+    });
+}
+
+int heffte_gb300_plan_destroy(heffte_gb300_plan plan){ return guard([&]{ delete plan; }); }
+
+int heffte_gb300_plan_set_stream(heffte_gb300_plan plan, void *stream){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan");
+        plan->p->stream = as_stream(stream);
+    });
+}
+
+long long heffte_gb300_size_inbox(heffte_gb300_plan plan){ return plan ? plan->p->size_inbox() : -1; }
+long long heffte_gb300_size_outbox(heffte_gb300_plan plan){ return plan ? plan->p->size_outbox() : -1; }
+long long heffte_gb300_size_workspace(heffte_gb300_plan plan){ return plan ? plan->p->size_workspace() : -1; }
+double heffte_gb300_scale_factor(heffte_gb300_plan plan, int scale){ return plan ? plan->p->get_scale(scale) : 0.0; }
+
+static int exec(heffte_gb300_plan plan, bool fwd, int batch, int prec, const void *in, void *out, void *work, int scale){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan");
+        plan->p->execute(fwd, prec, batch, in, out, work, scale);
+        check_cuda(cudaPeekAtLastError(), fwd ? "forward transform" : "backward transform");
+    });
+}
+
+int heffte_gb300_forward(heffte_gb300_plan plan, int prec, const void *input, void *output, void *workspace, int scale){
+    return exec(plan, true, 1, prec, input, output, workspace, scale);
+}
+int heffte_gb300_backward(heffte_gb300_plan plan, int prec, const void *input, void *output, void *workspace, int scale){
+    return exec(plan, false, 1, prec, input, output, workspace, scale);
+}
+int heffte_gb300_forward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
+                               void *workspace, int scale){
+    return exec(plan, true, batch, prec, input, output, workspace, scale);
+}
+int heffte_gb300_backward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
+                                void *workspace, int scale){
+    return exec(plan, false, batch, prec, input, output, workspace, scale);
+}
+
+} // extern "C"

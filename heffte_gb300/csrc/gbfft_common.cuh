@@ -1,0 +1,212 @@
+// Shared definitions of the GB300 fft3d backend: complex helpers, the
+// device-side plan of one batched 1-D transform, radix butterflies.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbfft {
+
+template<typename T> struct cplx;
+template<> struct cplx<float>  { using type = float2; };
+template<> struct cplx<double> { using type = double2; };
+template<typename T> using c_t = typename cplx<T>::type;
+
+template<typename T> __host__ __device__ __forceinline__ c_t<T> mk(T re, T im){ c_t<T> r; r.x = re; r.y = im; return r; }
+template<typename C> __device__ __forceinline__ C cadd(C a, C b){ C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template<typename C> __device__ __forceinline__ C csub(C a, C b){ C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template<typename C> __device__ __forceinline__ C cmul(C a, C b){
+    C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// a * conj(b)
+template<typename C> __device__ __forceinline__ C cmulc(C a, C b){
+    C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
+}
+template<typename C> __device__ __forceinline__ C cconj(C a){ C r; r.x = a.x; r.y = -a.y; return r; }
+// multiply by -i (forward) or +i (backward)
+template<bool FWD, typename C> __device__ __forceinline__ C rot90(C a){
+    C r;
+    if (FWD){ r.x = a.y; r.y = -a.x; } else { r.x = -a.y; r.y = a.x; }
+    return r;
+}
+template<typename C, typename T> __device__ __forceinline__ C cscale(C a, T s){ C r; r.x = a.x * s; r.y = a.y * s; return r; }
+
+// --------------------------------------------------------------------------
+// Plan of one batched 1-D transform as seen by the kernels.
+// --------------------------------------------------------------------------
+constexpr int kMaxStages = 16;
+
+struct Stage {
+    int R;          // radix
+    int Ns;         // product of the radices of the previous stages
+    int NR;         // N / R (butterflies per transform)
+    int tw;         // offset of this stage's twiddles in the table
+    uint32_t mul;   // j / Ns = (umulhi(j, mul) + j) >> shift
+    int shift;
+};
+
+struct Plan1D {
+    int N;          // transform length
+    int T;          // threads per transform
+    int nstages;
+    Stage st[kMaxStages];
+};
+
+// Layout of a batch of G transforms of length N inside an array:
+//   element p of transform g sits at  (g / count) * bstride + (g % count) * dist + p * estride.
+struct Layout {
+    long long count, dist, bstride, estride;
+};
+
+__device__ __forceinline__ long long base_of(Layout const &L, long long g){
+    return (g / L.count) * L.bstride + (g % L.count) * L.dist;
+}
+
+__device__ __forceinline__ int fdiv(int j, Stage const &s){
+    return (int)((__umulhi((uint32_t)j, s.mul) + (uint32_t)j) >> s.shift);
+}
+
+// Radix constants cos/sin(2 pi m / P) for the odd prime radices P (values of
+// the mathematical constants, written out in decimal).  Called with
+// compile-time arguments after unrolling, so the switch folds away.
+__host__ __device__ __forceinline__ constexpr double prime_cs(int P, int m, bool sine){
+    switch (P * 100 + m){
+        case 301: return sine ? 0.86602540378443864676 : -0.5;
+        case 501: return sine ? 0.95105651629515353118 : 0.30901699437494745126;
+        case 502: return sine ? 0.58778525229247324813 : -0.80901699437494734024;
+        case 701: return sine ? 0.78183148246802980363 : 0.62348980185873359439;
+        case 702: return sine ? 0.97492791218182361934 : -0.22252093395631433737;
+        case 703: return sine ? 0.43388373911755823142 : -0.90096886790241903498;
+        case 1101: return sine ? 0.54064081745559755543 : 0.84125353283118120551;
+        case 1102: return sine ? 0.90963199535451833011 : 0.41541501300188643508;
+        case 1103: return sine ? 0.98982144188093279524 : -0.14231483827328500480;
+        case 1104: return sine ? 0.75574957435425826890 : -0.65486073394528498959;
+        case 1105: return sine ? 0.28173255684142967104 : -0.95949297361449736865;
+        case 1301: return sine ? 0.46472317204376850652 : 0.88545602565320991051;
+        case 1302: return sine ? 0.82298386589365635224 : 0.56806474673115592289;
+        case 1303: return sine ? 0.99270887409805397272 : 0.12053668025532300601;
+        case 1304: return sine ? 0.93501624268541483342 : -0.35460488704253545489;
+        case 1305: return sine ? 0.66312265824079519305 : -0.74851074817110119231;
+        case 1306: return sine ? 0.23931566428755768339 : -0.97094181742605201180;
+        default: return 0.0;
+    }
+}
+
+// Odd prime radix P: y_q = sum_r v_r w^(q r), w = exp(-+ 2 pi i / P).
+template<int P, bool FWD, typename C, typename T>
+__device__ __forceinline__ void bfly_prime(C *v){
+    constexpr int H = (P - 1) / 2;
+    C a[H], b[H];
+    C v0 = v[0];
+    C y0 = v0;
+    #pragma unroll
+    for (int r = 1; r <= H; r++){
+        a[r - 1] = cadd(v[r], v[P - r]);
+        b[r - 1] = csub(v[r], v[P - r]);
+        y0 = cadd(y0, a[r - 1]);
+    }
+    #pragma unroll
+    for (int q = 1; q <= H; q++){
+        C re = v0, im; im.x = 0; im.y = 0;
+        #pragma unroll
+        for (int r = 1; r <= H; r++){
+            int m = (q * r) % P;             // angle index in [1, P-1]
+            int mm = (m <= H) ? m : P - m;    // cos symmetric, sin antisymmetric
+            T c = (T)prime_cs(P, mm, false);
+            T s = (m <= H) ? (T)prime_cs(P, mm, true) : -(T)prime_cs(P, mm, true);
+            re.x += a[r - 1].x * c; re.y += a[r - 1].y * c;
+            im.x += b[r - 1].x * s; im.y += b[r - 1].y * s;
+        }
+        // forward: y_q = re - i*im, y_{P-q} = re + i*im (backward swaps)
+        C t; t.x = im.y; t.y = -im.x;   // -i * im
+        if (FWD){ v[q] = cadd(re, t); v[P - q] = csub(re, t); }
+        else    { v[q] = csub(re, t); v[P - q] = cadd(re, t); }
+    }
+    v[0] = y0;
+}
+
+template<int R, bool FWD, typename C, typename T>
+__device__ __forceinline__ void bfly(C *v){
+    if constexpr (R == 1){
+        return;
+    } else if constexpr (R == 2){
+        C a = v[0], b = v[1];
+        v[0] = cadd(a, b); v[1] = csub(a, b);
+    } else if constexpr (R == 4){
+        C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        C c = cadd(v[1], v[3]), d = rot90<FWD>(csub(v[1], v[3]));
+        v[0] = cadd(a, c); v[2] = csub(a, c);
+        v[1] = cadd(b, d); v[3] = csub(b, d);
+    } else if constexpr (R == 8){
+        const T h = (T)0.70710678118654752440;
+        // radix-2 split into even/odd radix-4 transforms
+        C e[4] = {v[0], v[2], v[4], v[6]};
+        C o[4] = {v[1], v[3], v[5], v[7]};
+        bfly<4, FWD, C, T>(e);
+        bfly<4, FWD, C, T>(o);
+        // o[k] *= w8^k
+        C o1 = o[1], o3 = o[3];
+        if (FWD){
+            o[1].x = h * (o1.x + o1.y); o[1].y = h * (o1.y - o1.x);
+            o[3].x = h * (o3.y - o3.x); o[3].y = -h * (o3.x + o3.y);
+        } else {
+            o[1].x = h * (o1.x - o1.y); o[1].y = h * (o1.y + o1.x);
+            o[3].x = -h * (o3.x + o3.y); o[3].y = h * (o3.x - o3.y);
+        }
+        o[2] = rot90<FWD>(o[2]);
+        #pragma unroll
+        for (int k = 0; k < 4; k++){ v[k] = cadd(e[k], o[k]); v[k + 4] = csub(e[k], o[k]); }
+    } else if constexpr (R == 16){
+        // 4 x 4: columns, internal twiddles w16^(k1 n2), rows
+        const T c1 = (T)0.92387953251128675613, s1 = (T)0.38268343236508977173, h = (T)0.70710678118654752440;
+        C x[16];
+        #pragma unroll
+        for (int n2 = 0; n2 < 4; n2++){
+            C t[4] = {v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]};
+            bfly<4, FWD, C, T>(t);
+            #pragma unroll
+            for (int k1 = 0; k1 < 4; k1++) x[k1 * 4 + n2] = t[k1];
+        }
+        // twiddles w16^(k1*n2): exponents 0..9
+        auto tw = [&](C a, int e) -> C {
+            // multiply by exp(-+ 2 pi i e / 16)
+            C r;
+            T cs, sn;
+            switch (e){
+                case 1: cs = c1; sn = s1; break;
+                case 2: cs = h; sn = h; break;
+                case 3: cs = s1; sn = c1; break;
+                case 4: cs = 0; sn = 1; break;
+                case 6: cs = -h; sn = h; break;
+                case 9: cs = -c1; sn = -s1; break;
+                default: cs = 1; sn = 0; break;
+            }
+            if (FWD) sn = -sn;
+            r.x = a.x * cs - a.y * sn; r.y = a.x * sn + a.y * cs;
+            return r;
+        };
+        #pragma unroll
+        for (int k1 = 1; k1 < 4; k1++){
+            #pragma unroll
+            for (int n2 = 1; n2 < 4; n2++) x[k1 * 4 + n2] = tw(x[k1 * 4 + n2], k1 * n2);
+        }
+        #pragma unroll
+        for (int k1 = 0; k1 < 4; k1++){
+            C t[4] = {x[k1 * 4 + 0], x[k1 * 4 + 1], x[k1 * 4 + 2], x[k1 * 4 + 3]};
+            bfly<4, FWD, C, T>(t);
+            #pragma unroll
+            for (int k2 = 0; k2 < 4; k2++) v[k1 + 4 * k2] = t[k2];
+        }
+    } else if constexpr (R == 3){
+        bfly_prime<3, FWD, C, T>(v);
+    } else if constexpr (R == 5){
+        bfly_prime<5, FWD, C, T>(v);
+    } else if constexpr (R == 7){
+        bfly_prime<7, FWD, C, T>(v);
+    } else if constexpr (R == 11){
+        bfly_prime<11, FWD, C, T>(v);
+    } else if constexpr (R == 13){
+        bfly_prime<13, FWD, C, T>(v);
+    }
+}
+
+} // namespace gbfft

@@ -1,0 +1,263 @@
+// Host side of one transform length: radix plan, FP64-generated twiddle
+// tables, launch geometry of the batched kernels.
+#include "gbfft_internal.h"
+#include <map>
+#include <math.h>
+
+namespace gbfft {
+
+int num_sms(){
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    int &c = cached[dev & 63];
+    if (c == 0){
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        c = v;
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// Twiddle tables, computed in FP64 on the device and rounded once.
+// ---------------------------------------------------------------------------
+template<typename T>
+__global__ void k_stockham_twiddles(Plan1D P, c_t<T> *tw){
+    for (int s = 1; s < P.nstages; s++){
+        Stage S = P.st[s];
+        int n = S.Ns * (S.R - 1);
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x){
+            int k = idx / (S.R - 1), q = idx % (S.R - 1) + 1;
+            double sn, cs;
+            // exp(-2 pi i q k / (Ns R)); q k < Ns R so the ratio is exact-ish in FP64
+            sincospi(-2.0 * (double)(q * k) / (double)(S.Ns * S.R), &sn, &cs);
+            tw[S.tw + idx] = mk<T>((T)cs, (T)sn);
+        }
+    }
+}
+
+template<typename T>
+__global__ void k_r2r_twiddles(int N, c_t<T> *tw){
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x){
+        double sn, cs;
+        sincospi(-(double)k / (2.0 * (double)N), &sn, &cs);
+        tw[k] = mk<T>((T)cs, (T)sn);
+    }
+}
+
+Fft1D::~Fft1D(){
+    // tables live until process exit in the shared registry; freeing at
+    // static destruction time may run after the CUDA runtime is torn down
+}
+
+void const *Fft1D::twiddles(int prec, cudaStream_t s){
+    std::lock_guard<std::mutex> lk(mu);
+    if (!tw[prec]){
+        size_t es = (prec == 0) ? sizeof(float2) : sizeof(double2);
+        long long cnt = std::max<long long>(tw_count, 1);
+        check_cuda(cudaMalloc(&tw[prec], cnt * es), "cudaMalloc(twiddles)");
+        if (tw_count > 0){
+            int blocks = (int)std::min<long long>((tw_count + 255) / 256, 1024);
+            if (prec == 0) k_stockham_twiddles<float><<<blocks, 256, 0, s>>>(plan, (float2*)tw[prec]);
+            else k_stockham_twiddles<double><<<blocks, 256, 0, s>>>(plan, (double2*)tw[prec]);
+            check_cuda(cudaPeekAtLastError(), "twiddle kernel");
+        }
+    }
+    return tw[prec];
+}
+
+void const *Fft1D::r2r_twiddles(int prec, cudaStream_t s){
+    std::lock_guard<std::mutex> lk(mu);
+    if (!rtw[prec]){
+        size_t es = (prec == 0) ? sizeof(float2) : sizeof(double2);
+        check_cuda(cudaMalloc(&rtw[prec], N * es), "cudaMalloc(r2r twiddles)");
+        int blocks = std::min((N + 255) / 256, 1024);
+        if (prec == 0) k_r2r_twiddles<float><<<blocks, 256, 0, s>>>(N, (float2*)rtw[prec]);
+        else k_r2r_twiddles<double><<<blocks, 256, 0, s>>>(N, (double2*)rtw[prec]);
+        check_cuda(cudaPeekAtLastError(), "r2r twiddle kernel");
+    }
+    return rtw[prec];
+}
+
+// ---------------------------------------------------------------------------
+// Radix plans
+// ---------------------------------------------------------------------------
+static const int kRadices[] = {16, 13, 11, 8, 7, 5, 4, 3, 2};
+
+int max_length(int prec){
+    // one transform must fit in shared memory and T = N / kEmax threads <= 512
+    return (prec == 0) ? 8192 : 8192;
+}
+
+std::vector<int> default_radices(int N){
+    std::vector<int> r;
+    int n = N;
+    for (int p : {13, 11, 7, 5, 3}){
+        while (n % p == 0){ r.push_back(p); n /= p; }
+    }
+    int a = 0;
+    while (n % 2 == 0){ n /= 2; a++; }
+    if (n != 1) return {};  // a prime factor without a butterfly
+    // powers of two: as many radix-16 stages as possible, remainder 8/4 (or 8x4 for 2^1 with a 16 to spare)
+    std::vector<int> p2;
+    int q = a / 4, rem = a % 4;
+    if (rem == 1 && q >= 1){ q -= 1; p2.push_back(8); p2.push_back(4); }
+    else if (rem == 1) p2.push_back(2);
+    else if (rem == 2) p2.push_back(4);
+    else if (rem == 3) p2.push_back(8);
+    for (int i = 0; i < q; i++) p2.insert(p2.begin(), 16);
+    // radix-16 stages first, odd primes after
+    std::vector<int> out = p2;
+    out.insert(out.end(), r.begin(), r.end());
+    return out;
+}
+
+static void fast_div_params(int d, uint32_t &mul, int &shift){
+    int l = 0;
+    while ((1LL << l) < d) l++;
+    unsigned long long m = ((1ULL << 32) * ((1ULL << l) - (unsigned long long)d)) / (unsigned long long)d + 1ULL;
+    mul = (uint32_t)m;
+    shift = l;
+}
+
+static Plan1D build_plan(int N, std::vector<int> const &radices, long long &tw_count){
+    Plan1D P{};
+    P.N = N;
+    P.nstages = (int)radices.size();
+    if (P.nstages > kMaxStages) throw Error(ST_UNSUPPORTED, "too many radix stages");
+    int Ns = 1, off = 0, T = 1;
+    for (int s = 0; s < P.nstages; s++){
+        int R = radices[s];
+        Stage &S = P.st[s];
+        S.R = R; S.Ns = Ns; S.NR = N / R; S.tw = off;
+        fast_div_params(Ns, S.mul, S.shift);
+        if (s > 0) off += Ns * (R - 1);
+        int per = kEmax / R;
+        T = std::max(T, (S.NR + per - 1) / per);
+        Ns *= R;
+    }
+    if (Ns != N && N != 1) throw Error(ST_INVALID, "radix plan does not multiply to N");
+    P.T = T;
+    tw_count = off;
+    return P;
+}
+
+bool supported_length(int N, int prec){
+    if (N < 1 || N > max_length(prec)) return false;
+    if (N == 1) return true;
+    return !default_radices(N).empty();
+}
+
+std::shared_ptr<Fft1D> get_fft1d(int N, std::vector<int> const &radices){
+    static std::mutex mu;
+    static std::map<std::pair<int, std::vector<int>>, std::shared_ptr<Fft1D>> reg;
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(N, radices);
+    auto it = reg.find(key);
+    if (it != reg.end()) return it->second;
+    std::vector<int> rad = radices.empty() ? default_radices(N) : radices;
+    if (N != 1 && rad.empty())
+        throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(N) +
+                    " has a prime factor above 13, which this backend does not support");
+    long long prod = 1;
+    for (int r : rad){
+        bool ok = false;
+        for (int k : kRadices) ok = ok || (k == r);
+        if (!ok) throw Error(ST_INVALID, "unsupported radix " + std::to_string(r));
+        prod *= r;
+    }
+    if (N != 1 && prod != N) throw Error(ST_INVALID, "radix plan does not multiply to N");
+    auto f = std::make_shared<Fft1D>();
+    f->N = N;
+    f->radices = rad;
+    if (N == 1) f->radices.clear();
+    f->plan = build_plan(N, f->radices, f->tw_count);
+    reg[key] = f;
+    return f;
+}
+
+// ---------------------------------------------------------------------------
+// Launch geometry
+// ---------------------------------------------------------------------------
+static void geometry(Fft1D &f, int prec, bool cols, bool paired, long long G, LaunchCfg cfg, KernelArgs &a){
+    int N = f.N, T = f.plan.T;
+    size_t ce = (prec == 0) ? sizeof(float2) : sizeof(double2);
+    size_t unit = cols ? (size_t)N * ce : (size_t)(N + (N >> 4) + 1) * ce;
+    long long units = paired ? (G + 1) / 2 : G;
+    int tpb;
+    if (cfg.tpb > 0) tpb = cfg.tpb;
+    else if (cols) tpb = std::max((prec == 0) ? (paired ? 16 : 16) : 8, (256 + T - 1) / T);
+    else tpb = std::max(1, 256 / T);
+    tpb = std::min(tpb, std::max(1, 512 / T));
+    size_t budget = 100 * 1024;
+    while (tpb > 1 && (size_t)tpb * unit > budget) tpb--;
+    if ((size_t)tpb * unit > 227 * 1024) throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(N) + " does not fit in shared memory");
+    if (units < tpb) tpb = (int)std::max<long long>(units, 1);
+    a.tpb = tpb;
+    a.threads = tpb * T;
+    a.smem = (size_t)tpb * unit;
+    a.blocks = (units + tpb - 1) / tpb;
+    a.plan = &f.plan;
+    a.G = G;
+}
+
+static void run(cudaStream_t s, int kind, int prec, bool cols, KernelArgs &a){
+    if (a.blocks <= 0) return;
+    if (a.blocks > 0x7fffffffLL) throw Error(ST_UNSUPPORTED, "batch too large for one launch");
+    if (prec == 0) launch_kernel_f32(s, kind, cols, a); else launch_kernel_f64(s, kind, cols, a);
+}
+
+static bool is_cols(Layout const &Li, Layout const &Lo){ return !(Li.estride == 1 && Lo.estride == 1); }
+
+void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
+                long long G, double scale, LaunchCfg cfg){
+    if (G <= 0) return;
+    KernelArgs a{};
+    bool cols = is_cols(Li, Lo);
+    geometry(f, prec, cols, false, G, cfg, a);
+    a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
+    a.tw = f.twiddles(prec, s);
+    a.scale = scale; a.do_scale = (scale != 1.0);
+    run(s, fwd ? K_C2C_F : K_C2C_B, prec, cols, a);
+}
+
+void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
+                long long G, double scale, LaunchCfg cfg){
+    if (G <= 0) return;
+    KernelArgs a{};
+    bool cols = is_cols(Li, Lo);
+    geometry(f, prec, cols, true, G, cfg, a);
+    a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
+    a.tw = f.twiddles(prec, s);
+    a.scale = scale; a.do_scale = (scale != 1.0);
+    run(s, K_R2C, prec, cols, a);
+}
+
+void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
+                long long G, double scale, LaunchCfg cfg){
+    if (G <= 0) return;
+    KernelArgs a{};
+    bool cols = is_cols(Li, Lo);
+    geometry(f, prec, cols, true, G, cfg, a);
+    a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
+    a.tw = f.twiddles(prec, s);
+    a.scale = scale; a.do_scale = (scale != 1.0);
+    run(s, K_C2R, prec, cols, a);
+}
+
+void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout Li, Layout Lo, void const *in,
+                void *out, long long G, double scale, LaunchCfg cfg){
+    if (G <= 0) return;
+    KernelArgs a{};
+    bool cols = is_cols(Li, Lo);
+    geometry(f, prec, cols, true, G, cfg, a);
+    a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
+    a.tw = f.twiddles(prec, s);
+    a.rtw = f.r2r_twiddles(prec, s);
+    a.scale = scale; a.do_scale = (scale != 1.0);
+    a.sine = sine ? 1 : 0;
+    run(s, fwd ? K_R2R_F : K_R2R_B, prec, cols, a);
+}
+
+} // namespace gbfft

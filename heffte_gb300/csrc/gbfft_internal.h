@@ -1,0 +1,102 @@
+// Host-side internals shared by the translation units of libheffte_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <algorithm>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include "gbfft_common.cuh"
+
+namespace gbfft {
+
+enum DType { DT_FLOAT = 0, DT_DOUBLE = 1, DT_CFLOAT = 2, DT_CDOUBLE = 3 };
+
+// Error raised inside the library; the C-ABI turns it into a status code and
+// a message readable through heffte_gb300_last_error().
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, std::string const &m) : std::runtime_error(m), code(c) {}
+};
+enum { ST_OK = 0, ST_INVALID = 1, ST_CUDA = 2, ST_UNSUPPORTED = 3, ST_ALLOC = 4, ST_TIMEOUT = 5 };
+
+inline void check_cuda(cudaError_t e, char const *what){
+    if (e != cudaSuccess) throw Error(ST_CUDA, std::string(what) + " failed with message: " + cudaGetErrorString(e));
+}
+
+int num_sms();
+int elem_size(int dtype);
+
+// ---------------------------------------------------------------------------
+// 1-D transform length: radix plan, thread count and device twiddle tables.
+// ---------------------------------------------------------------------------
+constexpr int kEmax = 16;
+
+struct Fft1D {
+    int N = 0;
+    Plan1D plan{};
+    std::vector<int> radices;
+    // device tables, created lazily per precision: [0] float, [1] double
+    void *tw[2] = {nullptr, nullptr};     // Stockham twiddles
+    void *rtw[2] = {nullptr, nullptr};    // exp(-i pi k / 2N), k < N (r2r)
+    long long tw_count = 0;
+    std::mutex mu;
+    ~Fft1D();
+    void const *twiddles(int prec, cudaStream_t s);
+    void const *r2r_twiddles(int prec, cudaStream_t s);
+};
+
+// Shared registry of lengths (plans are immutable once built; tables lazily).
+// `radices` empty = default radix choice.
+std::shared_ptr<Fft1D> get_fft1d(int N, std::vector<int> const &radices = {});
+std::vector<int> default_radices(int N);
+bool supported_length(int N, int prec);
+int max_length(int prec);
+
+// Tuning knobs of one launch (chosen by the planner / autotuner).
+struct LaunchCfg {
+    int tpb = 0;   // transforms (or transform pairs) per CTA; 0 = automatic
+};
+
+// Batched 1-D launches (in units of elements of the respective arrays).
+void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
+                long long G, double scale, LaunchCfg cfg = {});
+void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
+                long long G, double scale, LaunchCfg cfg = {});
+void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
+                long long G, double scale, LaunchCfg cfg = {});
+void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout Li, Layout Lo, void const *in,
+                void *out, long long G, double scale, LaunchCfg cfg = {});
+
+// Location-layer data movement.
+void launch_direct_pack(cudaStream_t s, int dtype, long long nf, long long nm, long long ns, long long ls,
+                        long long ps, void const *src, void *dst, bool pack);
+void launch_transpose_unpack(cudaStream_t s, int dtype, long long nf, long long nm, long long ns, long long ls,
+                             long long ps, long long bls, long long bps, int m0, int m1, void const *src, void *dst);
+void launch_scale(cudaStream_t s, int prec, long long n, void *data, double factor);
+void launch_convert(cudaStream_t s, int prec, long long n, void const *src, void *dst, bool to_complex);
+
+// Per-precision kernel launchers (defined in gbfft_fft_f32.cu / _f64.cu).
+struct KernelArgs {
+    Plan1D const *plan;
+    Layout Li, Lo;
+    void const *in;
+    void *out;
+    void const *tw;
+    void const *rtw;
+    long long G;        // number of transforms (real transforms for the paired kernels)
+    int tpb;
+    int threads;
+    size_t smem;
+    long long blocks;
+    double scale;
+    int do_scale;
+    int sine;
+};
+enum Kind { K_C2C_F, K_C2C_B, K_R2C, K_C2R, K_R2R_F, K_R2R_B };
+void launch_kernel_f32(cudaStream_t s, int kind, bool cols, KernelArgs const &a);
+void launch_kernel_f64(cudaStream_t s, int kind, bool cols, KernelArgs const &a);
+
+} // namespace gbfft

@@ -1,0 +1,307 @@
+// Batched 1-D transform kernels for sm_103a (GB300).
+//
+// One CTA owns TPB transforms (TPB "lines" when the transform runs along the
+// fastest dimension, TPB adjacent "columns" when it runs along a strided
+// dimension) and T threads per transform.  The transform is a Stockham
+// autosort FFT whose radix sequence is a runtime list (radices 2, 3, 4, 5, 7,
+// 8, 11, 13, 16); each thread keeps up to EMAX complex values in registers:
+//   * stage 0 loads its butterfly inputs straight from HBM (coalesced: the
+//     Stockham input positions j + q*N/R are consecutive across threads, and
+//     in the column layout adjacent threads own adjacent columns);
+//   * middle stages exchange through shared memory (one read, one write);
+//   * the last stage stores straight to HBM (again positions j + q*N/R),
+//     or to shared memory when a fused post-processing step follows
+//     (r2c split, DCT/DST post-twiddle).
+// Twiddles come from a per-length table generated in FP64 on the device.
+#pragma once
+#include "gbfft_common.cuh"
+
+namespace gbfft {
+
+// Register file of one thread: EMAX complex values.
+template<typename T, int EMAX> struct Regs { c_t<T> v[EMAX]; };
+
+// Shared-memory index of element p of the local transform `loc`.
+template<bool COLS>
+__device__ __forceinline__ int sm_index(int p, int loc, int TPB, int padn){
+    return COLS ? (p * TPB + loc) : (loc * padn + p + (p >> 4));
+}
+
+template<int R, int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+__device__ __forceinline__ void fft_stage(Stage const &S, int t, int Tt, bool active, bool first, bool to_global,
+                                          c_t<T> *sm, int loc, int TPB, int padn,
+                                          c_t<T> const *__restrict__ tw, Regs<T, EMAX> &r, LD &ld, ST &st){
+    using C = c_t<T>;
+    constexpr int M = EMAX / R;
+    if (first){
+        #pragma unroll
+        for (int m = 0; m < M; m++){
+            int j = t + m * Tt;
+            if (active && j < S.NR){
+                #pragma unroll
+                for (int q = 0; q < R; q++) r.v[m * R + q] = ld(j + q * S.NR);
+            }
+        }
+    } else {
+        #pragma unroll
+        for (int m = 0; m < M; m++){
+            int j = t + m * Tt;
+            if (active && j < S.NR){
+                #pragma unroll
+                for (int q = 0; q < R; q++) r.v[m * R + q] = sm[sm_index<COLS>(j + q * S.NR, loc, TPB, padn)];
+            }
+        }
+        __syncthreads();
+    }
+    #pragma unroll
+    for (int m = 0; m < M; m++){
+        int j = t + m * Tt;
+        if (active && j < S.NR){
+            int hi = fdiv(j, S);
+            int k = j - hi * S.Ns;
+            if (!first && k != 0){
+                C const *w = tw + S.tw + k * (R - 1);
+                #pragma unroll
+                for (int q = 1; q < R; q++){
+                    C wq = __ldg(w + q - 1);
+                    r.v[m * R + q] = FWD ? cmul(r.v[m * R + q], wq) : cmulc(r.v[m * R + q], wq);
+                }
+            }
+            bfly<R, FWD, C, T>(&r.v[m * R]);
+            int ob = hi * S.Ns * R + k;
+            #pragma unroll
+            for (int q = 0; q < R; q++){
+                if (to_global) st(ob + q * S.Ns, r.v[m * R + q]);
+                else sm[sm_index<COLS>(ob + q * S.Ns, loc, TPB, padn)] = r.v[m * R + q];
+            }
+        }
+    }
+    if (!to_global) __syncthreads();
+}
+
+// Runs the whole transform. If last_to_global is false the result is left in
+// shared memory (natural order) and the CTA is synchronised on return.
+template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+__device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
+                                        c_t<T> const *__restrict__ tw, bool last_to_global, LD &ld, ST &st){
+    Regs<T, EMAX> r;
+    if (P.nstages == 0){
+        // length-1 transform: identity
+        if (active && t == 0){
+            c_t<T> x = ld(0);
+            if (last_to_global) st(0, x); else sm[sm_index<COLS>(0, loc, TPB, padn)] = x;
+        }
+        if (!last_to_global) __syncthreads();
+        return;
+    }
+    for (int s = 0; s < P.nstages; s++){
+        Stage const S = P.st[s];
+        bool first = (s == 0);
+        bool tg = (s == P.nstages - 1) && last_to_global;
+        switch (S.R){
+            case 16: if constexpr (EMAX >= 16) fft_stage<16, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 13: if constexpr (EMAX >= 13) fft_stage<13, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 11: if constexpr (EMAX >= 11) fft_stage<11, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 8: fft_stage<8, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 7: fft_stage<7, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 5: fft_stage<5, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 4: fft_stage<4, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 3: fft_stage<3, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            default: fft_stage<2, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+        }
+    }
+}
+
+// Thread -> (local transform, thread-in-transform) mapping.
+template<bool COLS>
+__device__ __forceinline__ void thread_map(int TPB, int Tt, int &loc, int &t){
+    int tid = threadIdx.x;
+    if (COLS){ loc = tid % TPB; t = tid / TPB; } else { loc = tid / Tt; t = tid % Tt; }
+}
+
+__device__ __forceinline__ int padded_len(int N){ return N + (N >> 4) + 1; }
+
+// ---------------------------------------------------------------------------
+// complex-to-complex
+// ---------------------------------------------------------------------------
+template<typename T, int EMAX, bool FWD, bool COLS>
+__global__ void __launch_bounds__(512)
+k_c2c(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
+      long long G, int TPB, T scale, int do_scale){
+    using C = c_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C*>(smraw);
+    int loc, t;
+    thread_map<COLS>(TPB, P.T, loc, t);
+    long long g = (long long)blockIdx.x * TPB + loc;
+    bool active = (g < G) && (t < P.T);
+    long long ib = active ? base_of(Li, g) : 0, ob = active ? base_of(Lo, g) : 0;
+    long long ies = Li.estride, oes = Lo.estride;
+    auto ld = [&](int p) -> C { return in[ib + p * ies]; };
+    auto st = [&](int p, C v){ out[ob + p * oes] = do_scale ? cscale(v, scale) : v; };
+    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+}
+
+// ---------------------------------------------------------------------------
+// real-to-complex: two real transforms (a = 2g, b = 2g+1) in one complex FFT,
+// z = x_a + i x_b; X_a[k] = (Z_k + conj Z_{N-k})/2, X_b[k] = -i (Z_k - conj Z_{N-k})/2.
+// Li is in real elements, Lo in complex elements; outputs k = 0..N/2.
+// ---------------------------------------------------------------------------
+template<typename T, int EMAX, bool COLS>
+__global__ void __launch_bounds__(512)
+k_r2c(Plan1D P, Layout Li, Layout Lo, T const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
+      long long G, int TPB, T scale, int do_scale){
+    using C = c_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C*>(smraw);
+    int loc, t;
+    thread_map<COLS>(TPB, P.T, loc, t);
+    long long gp = (long long)blockIdx.x * TPB + loc;
+    long long ga = 2 * gp, gb = 2 * gp + 1;
+    bool active = (ga < G) && (t < P.T);
+    bool hasb = gb < G;
+    long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
+    long long ies = Li.estride;
+    auto ld = [&](int p) -> C {
+        C z; z.x = in[ia + p * ies]; z.y = hasb ? in[ibb + p * ies] : (T)0; return z;
+    };
+    auto st = [&](int, C){};
+    int padn = padded_len(P.N);
+    fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, false, ld, st);
+    if (!active) return;
+    int N = P.N;
+    long long oa = base_of(Lo, ga), obb = hasb ? base_of(Lo, gb) : 0;
+    long long oes = Lo.estride;
+    T h = (T)0.5 * (do_scale ? scale : (T)1);
+    for (int k = t; k <= N / 2; k += P.T){
+        C zk = sm[sm_index<COLS>(k, loc, TPB, padn)];
+        int nk = (k == 0) ? 0 : N - k;
+        C zn = sm[sm_index<COLS>(nk, loc, TPB, padn)];
+        C xa; xa.x = h * (zk.x + zn.x); xa.y = h * (zk.y - zn.y);
+        out[oa + k * oes] = xa;
+        if (hasb){
+            // -i * (zk - conj zn) / 2
+            C xb; xb.x = h * (zk.y + zn.y); xb.y = -h * (zk.x - zn.x);
+            out[obb + k * oes] = xb;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// complex-to-real (unnormalised inverse): two half spectra in one complex FFT.
+// Z_p = X'_a[p] + i X'_b[p] with X'[p] = X[p] (p <= N/2, imaginary part of
+// the DC and Nyquist terms dropped) and conj X[N-p] above N/2.
+// ---------------------------------------------------------------------------
+template<typename T, int EMAX, bool COLS>
+__global__ void __launch_bounds__(512)
+k_c2r(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, T *out, c_t<T> const *__restrict__ tw,
+      long long G, int TPB, T scale, int do_scale){
+    using C = c_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C*>(smraw);
+    int loc, t;
+    thread_map<COLS>(TPB, P.T, loc, t);
+    long long gp = (long long)blockIdx.x * TPB + loc;
+    long long ga = 2 * gp, gb = 2 * gp + 1;
+    bool active = (ga < G) && (t < P.T);
+    bool hasb = gb < G;
+    long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
+    long long oa = active ? base_of(Lo, ga) : 0, obb = (active && hasb) ? base_of(Lo, gb) : 0;
+    long long ies = Li.estride, oes = Lo.estride;
+    int N = P.N;
+    auto ld = [&](int p) -> C {
+        int pp = (2 * p <= N) ? p : N - p;
+        bool cj = (2 * p > N);
+        bool real_only = (pp == 0) || (2 * pp == N);
+        C xa = in[ia + pp * ies];
+        C xb = hasb ? in[ibb + pp * ies] : mk<T>(0, 0);
+        if (real_only){ xa.y = 0; xb.y = 0; }
+        if (cj){ xa.y = -xa.y; xb.y = -xb.y; }
+        C z; z.x = xa.x - xb.y; z.y = xa.y + xb.x; return z;
+    };
+    auto st = [&](int p, C v){
+        T s = do_scale ? scale : (T)1;
+        out[oa + p * oes] = v.x * s;
+        if (hasb) out[obb + p * oes] = v.y * s;
+    };
+    fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+}
+
+// ---------------------------------------------------------------------------
+// real-to-real: DCT-II (forward, REDFT10) / 2 x DCT-III (backward, 2 x REDFT01)
+// by Makhoul's N-point reordering, two lines per complex FFT; the sine kinds
+// (RODFT10 / 2 x RODFT01) by the identities
+//   DST-II(x)[k]  = DCT-II((-1)^n x_n)[N-1-k]
+//   DST-III(y)[n] = (-1)^n DCT-III(y_rev)[n].
+// rtw holds exp(-i pi k / 2N), k = 0..N-1.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int makhoul_src(int p, int N){ return (2 * p < N) ? 2 * p : 2 * (N - 1 - p) + 1; }
+
+template<typename T, int EMAX, bool FWD, bool COLS>
+__global__ void __launch_bounds__(512)
+k_r2r(Plan1D P, Layout Li, Layout Lo, T const *in, T *out, c_t<T> const *__restrict__ tw,
+      c_t<T> const *__restrict__ rtw, long long G, int TPB, int sine, T scale, int do_scale){
+    using C = c_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C*>(smraw);
+    int loc, t;
+    thread_map<COLS>(TPB, P.T, loc, t);
+    long long gp = (long long)blockIdx.x * TPB + loc;
+    long long ga = 2 * gp, gb = 2 * gp + 1;
+    bool active = (ga < G) && (t < P.T);
+    bool hasb = gb < G;
+    long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
+    long long oa = active ? base_of(Lo, ga) : 0, obb = (active && hasb) ? base_of(Lo, gb) : 0;
+    long long ies = Li.estride, oes = Lo.estride;
+    int N = P.N;
+    int padn = padded_len(N);
+    T s = do_scale ? scale : (T)1;
+    if (FWD){
+        auto ld = [&](int p) -> C {
+            int n = makhoul_src(p, N);
+            T sg = (sine && (n & 1)) ? (T)-1 : (T)1;
+            C z; z.x = sg * in[ia + n * ies]; z.y = hasb ? sg * in[ibb + n * ies] : (T)0; return z;
+        };
+        auto st = [&](int, C){};
+        fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, false, ld, st);
+        if (!active) return;
+        for (int k = t; k < N; k += P.T){
+            C zk = sm[sm_index<COLS>(k, loc, TPB, padn)];
+            C zn = sm[sm_index<COLS>((k == 0) ? 0 : N - k, loc, TPB, padn)];
+            C w = __ldg(rtw + k);                       // exp(-i pi k / 2N)
+            // A = zk + conj zn, B = -i (zk - conj zn); Y = Re(w * A), Re(w * B)
+            T ax = zk.x + zn.x, ay = zk.y - zn.y;
+            T bx = zk.y + zn.y, by = -(zk.x - zn.x);
+            T ya = (w.x * ax - w.y * ay) * s;
+            T yb = (w.x * bx - w.y * by) * s;
+            int ko = sine ? (N - 1 - k) : k;
+            out[oa + ko * oes] = ya;
+            if (hasb) out[obb + ko * oes] = yb;
+        }
+    } else {
+        // V[k] = 2 exp(i pi k / 2N) (Y[k] - i Y[N-k]), Y[N] = 0; Z = V_a + i V_b.
+        auto yval = [&](long long base, int k) -> T {
+            if (k >= N) return (T)0;
+            int kk = sine ? (N - 1 - k) : k;
+            return in[base + kk * ies];
+        };
+        auto ld = [&](int p) -> C {
+            C w = __ldg(rtw + p); w.y = -w.y;             // exp(+i pi p / 2N)
+            T a0 = yval(ia, p), a1 = (p == 0) ? (T)0 : yval(ia, N - p);
+            T b0 = hasb ? yval(ibb, p) : (T)0, b1 = (hasb && p != 0) ? yval(ibb, N - p) : (T)0;
+            // V_a = 2 w (a0 - i a1), V_b = 2 w (b0 - i b1)
+            C va; va.x = 2 * (w.x * a0 + w.y * a1); va.y = 2 * (w.y * a0 - w.x * a1);
+            C vb; vb.x = 2 * (w.x * b0 + w.y * b1); vb.y = 2 * (w.y * b0 - w.x * b1);
+            C z; z.x = va.x - vb.y; z.y = va.y + vb.x; return z;
+        };
+        auto st = [&](int n, C v){
+            int m = makhoul_src(n, N);
+            T sg = (sine && (m & 1)) ? -s : s;
+            out[oa + m * oes] = v.x * sg;
+            if (hasb) out[obb + m * oes] = v.y * sg;
+        };
+        fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, true, ld, st);
+    }
+}
+
+} // namespace gbfft

@@ -1,0 +1,363 @@
+// Single-rank fft3d plan for the GB300 backend: stage sequencing of
+// compute_transform (src/heffte_compute_transform.cpp:15-258) and the setup
+// of fft3d / fft3d_r2c (include/heffte_fft3d.h:599-651,
+// include/heffte_fft3d_r2c.h:325-340), rebuilt around fused device passes:
+//   * every 1-D pass reads its source buffer and writes its destination
+//     directly (no copy_n of the input, no separate scale pass: the scale
+//     factor is folded into the last pass);
+//   * use_reorder = false runs strided passes in the input layout, the last
+//     pass writing the output box order directly;
+//   * use_reorder = true inserts transposes (transpose_unpack kernels) so that
+//     every pass runs along the fastest dimension, as reshape3d_transpose does
+//     (include/heffte_reshape3d.h:443-487).
+#include "gbfft_plan.h"
+#include <cmath>
+
+namespace gbfft {
+
+bool valid_order(std::array<int, 3> const &o){
+    return (o[0] != o[1] && o[0] != o[2] && o[1] != o[2] &&
+            o[0] >= 0 && o[0] < 3 && o[1] >= 0 && o[1] < 3 && o[2] >= 0 && o[2] < 3);
+}
+
+Layout pass_layout(Box3 const &box, int dim, std::array<int, 3> const &ref_order){
+    int a = -1, b = -1;
+    for (int i = 0; i < 3; i++){
+        int d = ref_order[i];
+        if (d == dim) continue;
+        if (a < 0) a = d; else b = d;
+    }
+    auto s = box.strides();
+    Layout L;
+    L.count = box.size[a];
+    L.dist = s[a];
+    L.bstride = s[b];
+    L.estride = s[dim];
+    return L;
+}
+
+static long long batch_count(Box3 const &box, int dim){ return box.count() / box.size[dim]; }
+
+// ---------------------------------------------------------------------------
+// executors
+// ---------------------------------------------------------------------------
+std::unique_ptr<Executor> make_executor(int kind, Box3 const &box, std::vector<int> const &dims){
+    if (box.empty()) return nullptr;
+    if (!valid_order(box.order)) throw Error(ST_INVALID, "invalid box order");
+    if (dims.empty() || dims.size() > 3) throw Error(ST_INVALID, "executor needs 1 to 3 dimensions");
+    if (kind == EX_R2C && dims.size() != 1) throw Error(ST_INVALID, "r2c executor works along one dimension");
+    auto e = std::make_unique<Executor>();
+    e->kind = kind;
+    e->box = box;
+    e->dims = dims;
+    for (int d : dims){
+        if (d < 0 || d > 2) throw Error(ST_INVALID, "invalid dimension");
+        if (!supported_length((int)box.size[d], 1))
+            throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(box.size[d]) + " is not supported");
+        e->ffts.push_back(get_fft1d((int)box.size[d]));
+    }
+    return e;
+}
+
+void Executor::forward(cudaStream_t s, int prec, void const *in, void *out, double scale) const{
+    if (kind == EX_R2C){
+        Box3 cb = box.r2c(dims[0]);
+        launch_r2c(s, *ffts[0], prec, pass_layout(box, dims[0], box.order), pass_layout(cb, dims[0], box.order),
+                   in, out, batch_count(box, dims[0]), scale);
+        return;
+    }
+    void const *src = in;
+    for (size_t i = 0; i < dims.size(); i++){
+        double sc = (i + 1 == dims.size()) ? scale : 1.0;
+        Layout L = pass_layout(box, dims[i], box.order);
+        if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, true, L, L, src, out, batch_count(box, dims[i]), sc);
+        else launch_r2r(s, *ffts[i], prec, true, kind == EX_SIN, L, L, src, out, batch_count(box, dims[i]), sc);
+        src = out;
+    }
+}
+
+void Executor::backward(cudaStream_t s, int prec, void const *in, void *out, double scale) const{
+    if (kind == EX_R2C){
+        Box3 cb = box.r2c(dims[0]);
+        launch_c2r(s, *ffts[0], prec, pass_layout(cb, dims[0], box.order), pass_layout(box, dims[0], box.order),
+                   in, out, batch_count(box, dims[0]), scale);
+        return;
+    }
+    void const *src = in;
+    for (size_t i = 0; i < dims.size(); i++){
+        double sc = (i + 1 == dims.size()) ? scale : 1.0;
+        Layout L = pass_layout(box, dims[i], box.order);
+        if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, false, L, L, src, out, batch_count(box, dims[i]), sc);
+        else launch_r2r(s, *ffts[i], prec, false, kind == EX_SIN, L, L, src, out, batch_count(box, dims[i]), sc);
+        src = out;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// plan construction
+// ---------------------------------------------------------------------------
+namespace {
+
+enum { B_IN = 0, B_OUT = 1, B_WA = 2, B_WB = 3 };
+
+struct PassSpec {
+    int kind;      // K_C2C_F ... (kernel kind)
+    int dim;
+};
+
+std::array<int, 3> order_with_first(std::array<int, 3> const &cur, int d){
+    std::array<int, 3> o{d, 0, 0};
+    int k = 1;
+    for (int i = 0; i < 3; i++) if (cur[i] != d) o[k++] = cur[i];
+    return o;
+}
+
+// Builds the op list for one direction.
+//   passes : the 1-D passes in execution order
+//   src_box: input box (with its order), dst_box: output box (with its order)
+//   inter  : box geometry of the intermediate (complex for r2c/c2r) data
+//   out_holds_inter: the output buffer has the element type of the intermediate data
+std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_box, Box3 const &dst_box,
+                          Box3 const &inter_geom, bool reorder, bool out_holds_inter, bool in_aliases_out,
+                          int &work_buffers){
+    // drop length-1 passes (identity), keep at least one op to move the data
+    std::vector<PassSpec> ps;
+    for (auto const &p : passes){
+        bool r2x = (p.kind == K_R2C || p.kind == K_C2R);
+        Box3 const &g = (p.kind == K_R2C) ? src_box : inter_geom;
+        if (g.size[p.dim] > 1 || r2x) ps.push_back(p);
+    }
+    std::vector<Op> ops;
+    // logical walk: current box (geometry + order) of the data
+    Box3 cur = src_box;
+    for (size_t i = 0; i < ps.size(); i++){
+        PassSpec const &p = ps[i];
+        if (reorder && cur.order[0] != p.dim){
+            Op r;
+            r.type = Op::RESHAPE;
+            r.sbox = cur;
+            r.dbox = cur.with_order(order_with_first(cur.order, p.dim));
+            ops.push_back(r);
+            cur = r.dbox;
+        }
+        Op f;
+        f.type = Op::FFT;
+        f.kind = p.kind;
+        f.dim = p.dim;
+        f.sbox = cur;
+        Box3 next = cur;
+        if (p.kind == K_R2C){
+            next = cur.r2c(p.dim);
+        } else if (p.kind == K_C2R){
+            next = dst_box.with_order(cur.order);
+        }
+        f.dbox = next;
+        f.ref_order = cur.order;
+        f.fft = get_fft1d((int)((p.kind == K_R2C) ? cur.size[p.dim] : (p.kind == K_C2R ? dst_box.size[p.dim] : cur.size[p.dim])));
+        ops.push_back(f);
+        cur = next;
+    }
+    if (ops.empty()){
+        Op c;
+        c.type = Op::COPY;
+        c.sbox = src_box;
+        c.dbox = dst_box;
+        ops.push_back(c);
+        cur = dst_box;
+    }
+    // mark the scale carrier: the last FFT (or the copy)
+    for (int i = (int)ops.size() - 1; i >= 0; i--){
+        if (ops[i].type != Op::RESHAPE){ ops[i].last = true; break; }
+    }
+    // final layout: the last op writes the output order directly (an FFT
+    // pass can write any order); a reorder plan ends with a transpose when
+    // its last pass leaves another order.
+    bool last_is_fft = ops.back().type != Op::RESHAPE;
+    if (reorder && cur.order != dst_box.order){
+        Op r;
+        r.type = Op::RESHAPE;
+        r.sbox = cur;
+        r.dbox = cur.with_order(dst_box.order);
+        ops.push_back(r);
+        last_is_fft = false;
+    } else if (last_is_fft){
+        ops.back().dbox = ops.back().dbox.with_order(dst_box.order);
+    }
+    (void)last_is_fft;
+    // buffer assignment
+    bool has_reshape = false;
+    for (auto const &o : ops) has_reshape = has_reshape || (o.type == Op::RESHAPE);
+    Op const &first = ops.front();
+    bool first_changes_layout = (first.type != Op::FFT) || first.kind == K_R2C || first.kind == K_C2R ||
+                                first.sbox.order != first.dbox.order;
+    bool orders_kept = true;
+    for (auto const &o : ops) orders_kept = orders_kept && (o.sbox.order == o.dbox.order);
+    bool x_is_out = !has_reshape && out_holds_inter && orders_kept && !(in_aliases_out && first_changes_layout);
+    int cur_buf = B_IN;
+    int used = 0;
+    for (size_t i = 0; i < ops.size(); i++){
+        Op &o = ops[i];
+        o.src = cur_buf;
+        bool final_op = (i + 1 == ops.size());
+        if (final_op || (x_is_out && o.type == Op::FFT)){
+            o.dst = B_OUT;
+        } else if (o.type == Op::FFT && cur_buf != B_IN && o.sbox.order == o.dbox.order){
+            o.dst = cur_buf;              // in place
+        } else {
+            o.dst = (cur_buf == B_WA) ? B_WB : B_WA;
+            used = std::max(used, (o.dst == B_WA) ? 1 : 2);
+        }
+        cur_buf = o.dst;
+    }
+    work_buffers = used;
+    return ops;
+}
+
+} // namespace
+
+std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbox, int r2c_dir, Options const &o,
+                                  cudaStream_t stream){
+    if (!valid_order(inbox.order) || !valid_order(outbox.order)) throw Error(ST_INVALID, "invalid box order");
+    if (inbox.empty()) throw Error(ST_INVALID, "empty input box");
+    auto p = std::make_unique<Plan3D>();
+    p->kind = kind;
+    p->inbox = inbox;
+    p->r2c_dir = r2c_dir;
+    p->opts = o;
+    p->stream = stream;
+    // single rank: the boxes are the whole world (heffte_fft3d.h:270-297 on MPI_COMM_SELF)
+    if (kind == PK_R2C){
+        if (r2c_dir < 0 || r2c_dir > 2) throw Error(ST_INVALID, "r2c_direction must be 0, 1 or 2");
+        Box3 expect = inbox.r2c(r2c_dir);
+        if (outbox.lo != expect.lo || outbox.hi != expect.hi)
+            throw Error(ST_INVALID, "on one rank the r2c output box must be inbox.r2c(r2c_direction)");
+    } else {
+        if (outbox.lo != inbox.lo || outbox.hi != inbox.hi)
+            throw Error(ST_INVALID, "on one rank the input and output boxes must cover the same indexes");
+    }
+    p->outbox = outbox;
+    for (int d = 0; d < 3; d++){
+        int n = (int)inbox.size[d];
+        if (!supported_length(n, 1))
+            throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(n) +
+                        " is not supported (lengths up to " + std::to_string(max_length(1)) +
+                        " with prime factors 2, 3, 5, 7, 11, 13)");
+    }
+    std::array<int, 3> io = inbox.order, oo = outbox.order;
+    bool reorder = o.use_reorder;
+    int wf = 0, wb = 0, wfa = 0;
+    if (kind == PK_C2C || kind == PK_COS || kind == PK_SIN){
+        bool r2r = (kind != PK_C2C);
+        std::vector<PassSpec> fwd, bwd;
+        for (int i = 0; i < 3; i++) fwd.push_back({r2r ? K_R2R_F : K_C2C_F, io[i]});
+        for (int i = 0; i < 3; i++) bwd.push_back({r2r ? K_R2R_B : K_C2C_B, oo[i]});
+        p->fwd = build_ops(fwd, inbox, outbox, inbox, reorder, true, false, wf);
+        p->fwd_alias = p->fwd;
+        p->bwd = build_ops(bwd, outbox, inbox, inbox, reorder, true, false, wb);
+        p->work_elems = std::max(wf, wb) * inbox.count();
+        double n = (double)inbox.count();
+        p->scale_factor = r2r ? 1.0 / (64.0 * n) : 1.0 / n;
+    } else {
+        Box3 cgeom = inbox.r2c(r2c_dir);
+        std::vector<PassSpec> fwd{{K_R2C, r2c_dir}}, bwd;
+        for (int i = 0; i < 3; i++) if (io[i] != r2c_dir) fwd.push_back({K_C2C_F, io[i]});
+        for (int i = 0; i < 3; i++) if (oo[i] != r2c_dir) bwd.push_back({K_C2C_B, oo[i]});
+        bwd.push_back({K_C2R, r2c_dir});
+        p->fwd = build_ops(fwd, inbox, outbox, cgeom, reorder, true, false, wf);
+        p->fwd_alias = build_ops(fwd, inbox, outbox, cgeom, reorder, true, true, wfa);
+        p->bwd = build_ops(bwd, outbox, inbox, cgeom, reorder, false, false, wb);
+        p->work_elems = std::max(std::max(wf, wfa), wb) * cgeom.count();
+        p->scale_factor = 1.0 / (double)inbox.count();
+    }
+    return p;
+}
+
+Plan3D::~Plan3D(){
+    if (cached_work) cudaFree(cached_work);
+}
+
+double Plan3D::get_scale(int scaling) const{
+    if (scaling == 0) return 1.0;
+    return (scaling == 2) ? std::sqrt(scale_factor) : scale_factor;
+}
+
+static int elem_dtype(int kind, int prec, bool complex_side){
+    if (kind == PK_COS || kind == PK_SIN) return prec == 0 ? DT_FLOAT : DT_DOUBLE;
+    if (complex_side) return prec == 0 ? DT_CFLOAT : DT_CDOUBLE;
+    return prec == 0 ? DT_FLOAT : DT_DOUBLE;
+}
+
+void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *out, void *work, int scaling){
+    if (prec != 0 && prec != 1) throw Error(ST_INVALID, "precision must be 0 (single) or 1 (double)");
+    if (scaling < 0 || scaling > 2) throw Error(ST_INVALID, "invalid scaling");
+    if (batch < 0) throw Error(ST_INVALID, "negative batch size");
+    if (batch == 0) return;
+    if (!in || !out) throw Error(ST_INVALID, "null input or output pointer");
+    // element types on each side
+    bool r2c = (kind == PK_R2C);
+    int in_dt = elem_dtype(kind, prec, r2c ? !forward : true);
+    int out_dt = elem_dtype(kind, prec, r2c ? forward : true);
+    int work_dt = elem_dtype(kind, prec, true);
+    size_t in_es = elem_size(in_dt), out_es = elem_size(out_dt), work_es = elem_size(work_dt);
+    long long in_cnt = forward ? size_inbox() : size_outbox();
+    long long out_cnt = forward ? size_outbox() : size_inbox();
+    bool alias = (in == out);
+    std::vector<Op> const &ops = forward ? (alias ? fwd_alias : fwd) : bwd;
+    // the workspace: 2 halves of work_elems/2 ... one box each
+    long long per_buf = (kind == PK_R2C) ? inbox.r2c(r2c_dir).count() : inbox.count();
+    size_t need = (size_t)work_elems * work_es;
+    char *wbase = reinterpret_cast<char*>(work);
+    if (need > 0 && !wbase){
+        if (cached_bytes < need){
+            if (cached_work) check_cuda(cudaFree(cached_work), "cudaFree(workspace)");
+            cached_work = nullptr;
+            cached_bytes = 0;
+            check_cuda(cudaMalloc(&cached_work, need), "cudaMalloc(workspace)");
+            cached_bytes = need;
+        }
+        wbase = reinterpret_cast<char*>(cached_work);
+    }
+    double sc = get_scale(scaling);
+    for (int j = 0; j < batch; j++){
+        void *bufs[4];
+        bufs[0] = const_cast<char*>(reinterpret_cast<char const*>(in)) + (size_t)j * in_cnt * in_es;
+        bufs[1] = reinterpret_cast<char*>(out) + (size_t)j * out_cnt * out_es;
+        bufs[2] = wbase;
+        bufs[3] = wbase ? wbase + (size_t)per_buf * work_es : nullptr;
+        for (auto const &op : ops){
+            void const *src = bufs[op.src];
+            void *dst = bufs[op.dst];
+            double s = op.last ? sc : 1.0;
+            if (op.type == Op::FFT){
+                Layout Li = pass_layout(op.sbox, op.dim, op.ref_order);
+                Layout Lo = pass_layout(op.dbox, op.dim, op.ref_order);
+                long long G = op.sbox.count() / op.sbox.size[op.dim];
+                switch (op.kind){
+                    case K_C2C_F: launch_c2c(stream, *op.fft, prec, true, Li, Lo, src, dst, G, s); break;
+                    case K_C2C_B: launch_c2c(stream, *op.fft, prec, false, Li, Lo, src, dst, G, s); break;
+                    case K_R2C: launch_r2c(stream, *op.fft, prec, Li, Lo, src, dst, G, s); break;
+                    case K_C2R: launch_c2r(stream, *op.fft, prec, Li, Lo, src, dst, G, s); break;
+                    case K_R2R_F: launch_r2r(stream, *op.fft, prec, true, kind == PK_SIN, Li, Lo, src, dst, G, s); break;
+                    case K_R2R_B: launch_r2r(stream, *op.fft, prec, false, kind == PK_SIN, Li, Lo, src, dst, G, s); break;
+                }
+            } else if (op.type == Op::RESHAPE){
+                Box3 const &A = op.sbox, &B = op.dbox;
+                int m[3];
+                for (int a = 0; a < 3; a++) m[a] = B.find_order(A.order[a]);
+                int dt = (op.src == 0) ? in_dt : ((op.dst == 1) ? out_dt : work_dt);
+                launch_transpose_unpack(stream, dt, B.osize(0), B.osize(1), B.osize(2), B.osize(0),
+                                        B.osize(0) * B.osize(1), A.osize(0), A.osize(0) * A.osize(1),
+                                        m[0], m[1], src, dst);
+            } else {
+                size_t bytes = (size_t)op.dbox.count() * out_es;
+                if (src != dst) check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, stream), "copy");
+                if (s != 1.0){
+                    long long reals = (long long)(bytes / ((prec == 0) ? 4 : 8));
+                    launch_scale(stream, prec, reals, dst, s);
+                }
+            }
+        }
+    }
+}
+
+} // namespace gbfft

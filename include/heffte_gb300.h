@@ -1,0 +1,189 @@
+/*
+ * heffte_gb300.h - C ABI of the GB300-native fft3d backend for heFFTe.
+ *
+ * A single-GPU, single-rank (MPI_COMM_SELF) drop-in for the device parts of
+ * heFFTe's fft3d hot path.  Plain C: opaque handles, raw device pointers,
+ * sizes as integers, a cudaStream_t passed as `void*` (NULL = default stream).
+ * Every function returns a status code (HEFFTE_GB300_SUCCESS = 0) and never
+ * throws; the message of the last failure on the calling thread is returned by
+ * heffte_gb300_last_error().  The reference turns every CUDA error into
+ * std::runtime_error("<call> failed with message: <text>")
+ * (include/heffte_backend_cuda.h:49-60); the reference-side shim in
+ * INTEGRATION.md rethrows our status the same way.
+ *
+ * Three layers, each replacing a reference interface:
+ *   1. location layer  -> src/heffte_backend_cuda.cu (cuda::convert, scale_data,
+ *                         direct_pack, direct_unpack, transpose_unpack);
+ *   2. executors       -> cufft_executor, cufft_executor_r2c and
+ *                         real2real_executor<cufft_cos|cufft_sin>;
+ *   3. 3-D plans       -> heffte::fft3d / fft3d_r2c / rtransform on one rank,
+ *                         shaped after the reference C API (include/heffte_c.h).
+ */
+#ifndef HEFFTE_GB300_H
+#define HEFFTE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define HEFFTE_GB300_SUCCESS 0
+#define HEFFTE_GB300_INVALID 1      /* bad geometry, null pointer, bad option   */
+#define HEFFTE_GB300_CUDA_ERROR 2   /* a CUDA runtime call or launch failed     */
+#define HEFFTE_GB300_UNSUPPORTED 3  /* e.g. a transform length with a prime > 13 */
+#define HEFFTE_GB300_ALLOC_ERROR 4  /* device allocation failed                  */
+
+/* element types: float, double, std::complex<float>, std::complex<double> */
+#define HEFFTE_GB300_FLOAT 0
+#define HEFFTE_GB300_DOUBLE 1
+#define HEFFTE_GB300_CFLOAT 2
+#define HEFFTE_GB300_CDOUBLE 3
+
+/* precision of a transform */
+#define HEFFTE_GB300_SINGLE 0
+#define HEFFTE_GB300_DOUBLE_PREC 1
+
+/* heffte::scale (include/heffte_fft3d.h:140-147), same values as heffte_c_defines.h */
+#define HEFFTE_GB300_SCALE_NONE 0
+#define HEFFTE_GB300_SCALE_FULL 1
+#define HEFFTE_GB300_SCALE_SYMMETRIC 2
+
+/* transform kinds: fft3d (c2c), fft3d_r2c, rtransform<cos> (DCT-II / 2xDCT-III),
+ * rtransform<sin> (DST-II / 2xDST-III) */
+#define HEFFTE_GB300_C2C 0
+#define HEFFTE_GB300_R2C 1
+#define HEFFTE_GB300_COS 2
+#define HEFFTE_GB300_SIN 3
+
+/* Message of the last failure on this thread ("" after a success). */
+const char *heffte_gb300_last_error(void);
+/* 10000*major + 100*minor + patch */
+int heffte_gb300_version(void);
+
+/* ======================================================================= */
+/* 1. Location layer                                                        */
+/* ======================================================================= */
+
+/* Replaces cuda::convert (src/heffte_backend_cuda.cu:345-361):
+ * to_complex = 1: dst[2i] = src[i], dst[2i+1] = 0 for i < n;
+ * to_complex = 0: dst[i] = src[2i].  prec 0 = float, 1 = double. */
+int heffte_gb300_convert(void *stream, int prec, long long n, const void *src, void *dst, int to_complex);
+
+/* Replaces cuda::scale_data (src/heffte_backend_cuda.cu:471-483):
+ * data[i] *= (scalar) factor for i < num_reals (complex data = 2n reals).
+ * num_reals = 0 is a no-op, as in the reference. */
+int heffte_gb300_scale_data(void *stream, int prec, long long num_reals, void *data, double factor);
+
+/* Replaces cuda::direct_pack (src/heffte_backend_cuda.cu:385-393), i.e.
+ * direct_packer<tag::gpu>::pack (include/heffte_backend_cuda.h:800-806):
+ * dst[(slow*nmid + mid)*nfast + fast] = src[slow*plane_stride + mid*line_stride + fast].
+ * dtype: HEFFTE_GB300_FLOAT .. HEFFTE_GB300_CDOUBLE.  Bit-exact copy. */
+int heffte_gb300_direct_pack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
+                             long long line_stride, long long plane_stride, const void *src, void *dst);
+
+/* Replaces cuda::direct_unpack (src/heffte_backend_cuda.cu:395-402): the inverse of direct_pack. */
+int heffte_gb300_direct_unpack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
+                               long long line_stride, long long plane_stride, const void *src, void *dst);
+
+/* Replaces cuda::transpose_unpack (src/heffte_backend_cuda.cu:404-441), i.e.
+ * transpose_packer<tag::gpu>::unpack (include/heffte_backend_cuda.h:824-828):
+ * dst[k*plane_stride + j*line_stride + i] = src[<map case>] for the six
+ * (map0, map1, map2) cases of the reference kernel (:90-133). Bit-exact. */
+int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
+                                  long long line_stride, long long plane_stride,
+                                  long long buff_line_stride, long long buff_plane_stride,
+                                  int map0, int map1, int map2, const void *src, void *dst);
+
+/* ======================================================================= */
+/* 2. Executors (one_dim_backend<tag>::executor / executor_r2c)             */
+/* ======================================================================= */
+
+typedef struct heffte_gb300_executor_s *heffte_gb300_executor;
+
+/* Creates a batched executor on the box {low, high, order}:
+ *   kind C2C: ndims = 1, 2 or 3 transform dimensions, the roles of the
+ *             cufft_executor constructors (include/heffte_backend_cuda.h:445-491);
+ *   kind R2C: ndims = 1, cufft_executor_r2c (:631-646);
+ *   kind COS / SIN: ndims = 1, real2real_executor<cufft_cos|cufft_sin>
+ *             (include/heffte_r2r_executor.h:191-210); unlike the reference
+ *             the dimension need not be the fastest one.
+ * An empty box gives *out = NULL and HEFFTE_GB300_SUCCESS, as make_executor
+ * returns a null pointer for empty boxes (include/heffte_common.h:669-676). */
+int heffte_gb300_executor_create(int kind, const long long low[3], const long long high[3], const int order[3],
+                                 int ndims, const int dims[3], heffte_gb300_executor *out);
+int heffte_gb300_executor_destroy(heffte_gb300_executor e);
+/* executor_base::box_size / complex_size / workspace_size (include/heffte_common.h:585-594) */
+long long heffte_gb300_executor_box_size(heffte_gb300_executor e);
+long long heffte_gb300_executor_complex_size(heffte_gb300_executor e);
+long long heffte_gb300_executor_workspace_size(heffte_gb300_executor e);
+/* Forward / backward.  C2C and COS/SIN: in-place when in == out (the
+ * reference signature forward(data[], workspace)); R2C forward: real in ->
+ * complex out; R2C backward: complex in -> real out (the input is not modified).
+ * prec 0 = single, 1 = double.  workspace may be NULL (size 0). */
+int heffte_gb300_executor_forward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
+                                  void *workspace);
+int heffte_gb300_executor_backward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
+                                   void *workspace);
+
+/* ======================================================================= */
+/* 3. 3-D plans: fft3d / fft3d_r2c / rtransform on one rank                 */
+/* ======================================================================= */
+
+/* plan_options (include/heffte_plan_logic.h:131-176), laid out as
+ * heffte_plan_options (include/heffte_c_defines.h:98-107). On one rank only
+ * use_reorder changes the device work: 1 = transpose so that every 1-D pass
+ * is contiguous (the reference's reshape3d_transpose), 0 = strided passes. */
+typedef struct {
+    int use_reorder;
+    int algorithm;
+    int use_pencils;
+    int use_gpu_aware;
+} heffte_gb300_plan_options;
+
+typedef struct heffte_gb300_plan_s *heffte_gb300_plan;
+
+/* Defaults of the GB300 tags: use_reorder = 0, alltoallv, pencils, gpu-aware
+ * (heffte_set_default_options, include/heffte_c.h:62). */
+int heffte_gb300_set_default_options(heffte_gb300_plan_options *options);
+
+/* heffte_plan_create / heffte_plan_create_r2c (include/heffte_c.h:78-105) for
+ * one rank: the boxes span the whole index set; *_order may be NULL for
+ * (0,1,2).  kind: HEFFTE_GB300_C2C, _R2C (outbox = inbox.r2c(r2c_direction)),
+ * _COS or _SIN.  stream: the cudaStream_t every call of this plan uses
+ * (NULL = default stream, a non-owning handle as in fft3d's constructor). */
+int heffte_gb300_plan_create(int kind, const int inbox_low[3], const int inbox_high[3], const int *inbox_order,
+                             const int outbox_low[3], const int outbox_high[3], const int *outbox_order,
+                             int r2c_direction, const heffte_gb300_plan_options *options, void *stream,
+                             heffte_gb300_plan *plan);
+int heffte_gb300_plan_destroy(heffte_gb300_plan plan);
+int heffte_gb300_plan_set_stream(heffte_gb300_plan plan, void *stream);
+
+/* fft3d::size_inbox / size_outbox / size_workspace (include/heffte_fft3d.h:324-331, :553-555).
+ * The workspace is counted in elements of the complex type (c2c, r2c) or of
+ * the real type (cos, sin). */
+long long heffte_gb300_size_inbox(heffte_gb300_plan plan);
+long long heffte_gb300_size_outbox(heffte_gb300_plan plan);
+long long heffte_gb300_size_workspace(heffte_gb300_plan plan);
+/* fft3d::get_scale_factor (include/heffte_fft3d.h:548-550) */
+double heffte_gb300_scale_factor(heffte_gb300_plan plan, int scale);
+
+/* fft3d::forward / backward with and without workspace
+ * (include/heffte_fft3d.h:353-542; heffte_forward_*, heffte_backward_*,
+ * include/heffte_c.h:140-256).  prec 0 = single, 1 = double.  Input is never
+ * modified.  workspace = NULL uses a buffer the plan allocates once and keeps
+ * (the reference allocates one per call).  batch > 1 transforms batch
+ * contiguous inputs (stride size_inbox) into contiguous outputs. */
+int heffte_gb300_forward(heffte_gb300_plan plan, int prec, const void *input, void *output, void *workspace,
+                         int scale);
+int heffte_gb300_backward(heffte_gb300_plan plan, int prec, const void *input, void *output, void *workspace,
+                          int scale);
+int heffte_gb300_forward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
+                               void *workspace, int scale);
+int heffte_gb300_backward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
+                                void *workspace, int scale);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,365 @@
+"""GPU parity of the CUDA path (through the C ABI) against the oracle.
+
+Bars: bit-exact for pack / unpack / transpose; rel-L2 <= 1e-6 (float) and
+<= 1e-12 (double) against the FP64 oracle for every transform; the reference's
+own float outputs (golden fixtures, stock<float>) within 5e-6 rel-L2.
+"""
+import numpy as np
+import pytest
+
+from oracle import heffte_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-6, 1: 1e-12}
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def cdt(prec):
+    return np.complex64 if prec == 0 else np.complex128
+
+
+def rdt(prec):
+    return np.float32 if prec == 0 else np.float64
+
+
+def rand_c(rng, n, prec):
+    return (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(cdt(prec))
+
+
+def run_c2c(gb, x, size, io, oo, direction, scaling, prec, reorder=0, workspace=False):
+    opts = gb.plan_options.default()
+    opts.use_reorder = reorder
+    ib = gb.box3d((0, 0, 0), [s - 1 for s in size], io)
+    ob = gb.box3d((0, 0, 0), [s - 1 for s in size], oo)
+    p = gb.fft3d(ib, ob, opts)
+    xin = dev(x)
+    y = torch.empty_like(xin)
+    if workspace:
+        w = torch.empty(max(p.size_workspace(), 1), dtype=xin.dtype, device="cuda")
+        (p.forward_buffered if direction == 0 else p.backward_buffered)(xin, y, w, scaling)
+    else:
+        (p.forward if direction == 0 else p.backward)(xin, y, scaling)
+    out = host(y)
+    assert np.array_equal(host(xin), x), "input modified"
+    return out
+
+
+# ---------------------------------------------------------------------------
+# location layer
+# ---------------------------------------------------------------------------
+def test_packers_bit_exact(gb, golden):
+    g = golden["packers"]
+    dtype_of = {4: 0, 8: 2, 16: 3}   # float, complex<float>, complex<double> words
+    for m in g["meta"]:
+        idx = int(m["idx"])
+        es = int(m["esize"])
+        src, dst, want = g[f"t{idx}_src"], g[f"t{idx}_dst"], g[f"t{idx}_out"]
+        s, d = dev(src), dev(dst)
+        size = (int(m["n0"]), int(m["n1"]), int(m["n2"]))
+        dt = dtype_of[es]
+        if m["op"] == "pack":
+            gb.direct_pack(dt, *size, int(m["ls"]), int(m["ps"]), s, d)
+        elif m["op"] == "unpack":
+            gb.direct_unpack(dt, *size, int(m["ls"]), int(m["ps"]), s, d)
+        else:
+            gb.transpose_unpack(dt, *size, int(m["ls"]), int(m["ps"]), int(m["bls"]), int(m["bps"]),
+                                (int(m["m0"]), int(m["m1"]), int(m["m2"])), s, d)
+        assert host(d).tobytes() == want.tobytes(), (str(m["op"]), idx, es)
+
+
+@pytest.mark.parametrize("mp", [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)])
+@pytest.mark.parametrize("dtype,np_t", [(0, np.float32), (2, np.complex64), (3, np.complex128)])
+def test_transpose_large_tiles_bit_exact(gb, mp, dtype, np_t):
+    """Transposes larger than one 32x32 tile, ragged edges, all six maps."""
+    rng = np.random.default_rng(5)
+    size = (67, 45, 33)
+    src_dims = [size[mp[a]] for a in range(3)]
+    bls, bps = src_dims[0], src_dims[0] * src_dims[1]
+    ls, ps = size[0] + 3, (size[0] + 3) * (size[1] + 2)
+    nsrc = int(np.prod(src_dims))
+    src = rng.standard_normal(nsrc * (2 if np.iscomplexobj(np.zeros(1, np_t)) else 1)).astype(
+        np.float32 if np_t in (np.float32, np.complex64) else np.float64).view(np_t)
+    dst = np.zeros(ps * size[2], np_t)
+    want = O.transpose_unpack(src, dst, size, ls, ps, bls, bps, mp)
+    s, d = dev(src), dev(dst)
+    gb.transpose_unpack(dtype, *size, ls, ps, bls, bps, mp, s, d)
+    assert host(d).tobytes() == want.tobytes()
+
+
+def test_direct_pack_unpack_roundtrip_bit_exact(gb):
+    rng = np.random.default_rng(9)
+    box = rng.standard_normal(40 * 30 * 20).astype(np.float64).view(np.complex128)  # 40*30*10 complex
+    size, ls, ps = (17, 13, 7), 40, 40 * 30
+    packed = O.direct_pack(box, size, ls, ps)
+    s = dev(box)
+    buf = torch.empty(int(np.prod(size)), dtype=torch.complex128, device="cuda")
+    gb.direct_pack(3, *size, ls, ps, s, buf)
+    assert host(buf).tobytes() == packed.tobytes()
+    back = torch.zeros_like(s)
+    gb.direct_unpack(3, *size, ls, ps, buf, back)
+    assert host(back).tobytes() == O.direct_unpack(packed, np.zeros_like(box), size, ls, ps).tobytes()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("n", [1, 7, 1000, 1 << 20])
+def test_scale_and_convert(gb, prec, n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n).astype(rdt(prec))
+    t = dev(x)
+    gb.scale_data(prec, n, t, 0.125)
+    assert np.array_equal(host(t), O.scale_data(x, 0.125, rdt(prec)))
+    c = torch.empty(2 * n, dtype=t.dtype, device="cuda")
+    gb.convert(prec, n, dev(x), c, True)
+    hc = host(c)
+    assert np.array_equal(hc[0::2], x) and not hc[1::2].any()
+    r = torch.empty(n, dtype=t.dtype, device="cuda")
+    gb.convert(prec, n, c, r, False)
+    assert np.array_equal(host(r), x)
+
+
+# ---------------------------------------------------------------------------
+# executors (the cufft_executor role)
+# ---------------------------------------------------------------------------
+def test_executor_known_answers(gb, golden):
+    ka = golden["known_answers"]
+    x = ka["input"].astype(np.complex128)
+    for d in range(3):
+        ex = gb.executor(gb.kind.c2c, gb.box3d((0, 0, 0), (1, 2, 3)), [d])
+        t = dev(x)
+        ex.forward(1, t, t)
+        assert np.allclose(host(t), ka[f"exec_dim{d}"], atol=1e-12)
+        ex.backward(1, t, t)
+        assert np.allclose(host(t), x * (2, 3, 4)[d], atol=1e-12)
+    for d in range(3):
+        ex = gb.executor(gb.kind.r2c, gb.box3d((0, 0, 0), (1, 2, 3)), [d])
+        r = dev(ka["input"])
+        c = torch.empty(ex.complex_size(), dtype=torch.complex128, device="cuda")
+        ex.forward(1, r, c)
+        want = O.from_canonical(np.take(np.fft.fft(O.to_canonical(ka["input"], (2, 3, 4), (0, 1, 2)), axis=2 - d),
+                                        np.arange((2, 3, 4)[d] // 2 + 1), axis=2 - d), (0, 1, 2))
+        assert np.allclose(host(c), want, atol=1e-12)
+
+
+@pytest.mark.parametrize("order", [(0, 1, 2), (2, 0, 1), (1, 2, 0)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_executor_each_dimension(gb, order, prec):
+    rng = np.random.default_rng(3)
+    size = (48, 20, 36)
+    n = int(np.prod(size))
+    x = rand_c(rng, n, prec)
+    for d in range(3):
+        ex = gb.executor(gb.kind.c2c, gb.box3d((0, 0, 0), [s - 1 for s in size], order), [d])
+        t = dev(x)
+        ex.forward(prec, t, t)
+        assert O.rel_l2(host(t), O.executor_c2c(x, size, order, d)) < TOL[prec]
+    ex = gb.executor(gb.kind.c2c, gb.box3d((0, 0, 0), [s - 1 for s in size], order), [0, 1, 2])
+    t = dev(x)
+    ex.forward(prec, t, t)
+    assert O.rel_l2(host(t), O.fft3d_c2c(x, size, order, order)) < TOL[prec]
+
+
+# ---------------------------------------------------------------------------
+# fft3d / fft3d_r2c / rtransform against the reference fixtures and the oracle
+# ---------------------------------------------------------------------------
+def test_known_answers_3d(gb, golden):
+    ka = golden["known_answers"]
+    x = ka["input"]
+    y = run_c2c(gb, x.astype(np.complex128), (2, 3, 4), (0, 1, 2), (0, 1, 2), 0, 0, 1)
+    assert np.allclose(y, ka["c2c_fwd"], atol=1e-11)
+    for kind, name in ((gb.kind.cos, "cos"), (gb.kind.sin, "sin")):
+        p = gb.rtransform(kind, gb.box3d((0, 0, 0), (1, 2, 3)), gb.box3d((0, 0, 0), (1, 2, 3)))
+        t = dev(x)
+        o = torch.empty_like(t)
+        p.forward(t, o)
+        assert np.allclose(host(o), ka[f"{name}_fwd"], atol=1e-10), name
+
+
+@pytest.mark.parametrize("reorder", [0, 1])
+def test_seeded_against_reference(gb, golden, reorder):
+    g = golden["seeded"]
+    for m in g["meta"]:
+        size = (int(m["n0"]), int(m["n1"]), int(m["n2"]))
+        io = (int(m["io0"]), int(m["io1"]), int(m["io2"]))
+        oo = (int(m["oo0"]), int(m["oo1"]), int(m["oo2"]))
+        prec = int(m["prec"])
+        key = str(m["key"])
+        x, fwd_ref, bwd_ref = g[key + "_in"], g[key + "_fwd"], g[key + "_bwd"]
+        opts = gb.plan_options.default()
+        opts.use_reorder = reorder
+        ib = gb.box3d((0, 0, 0), [s - 1 for s in size], io)
+        if m["kind"] == "c2c":
+            ob = gb.box3d((0, 0, 0), [s - 1 for s in size], oo)
+            p = gb.fft3d(ib, ob, opts)
+            want_f = O.fft3d_c2c(x, size, io, oo, 0)
+        elif m["kind"] == "r2c":
+            rd = int(m["r2c_dir"])
+            cb = ib.r2c(rd)
+            ob = gb.box3d(cb.low, cb.high, oo)
+            p = gb.fft3d_r2c(ib, ob, rd, opts)
+            want_f = O.fft3d_r2c(x, size, rd, io, oo)
+        else:
+            k = int(m["r2r_kind"])
+            if k == 2:
+                continue  # DCT-I is a later row
+            ob = gb.box3d((0, 0, 0), [s - 1 for s in size], oo)
+            p = gb.rtransform(gb.kind.cos if k == 0 else gb.kind.sin, ib, ob, opts)
+            want_f = O.rtransform(k, x, size, io, oo)
+        xin = dev(x)
+        y = torch.empty(p.size_outbox(), dtype=torch.from_numpy(fwd_ref[:1]).dtype, device="cuda")
+        p.forward(xin, y)
+        yf = host(y)
+        assert O.rel_l2(yf, want_f) < TOL[prec], (key, "fwd vs FP64", O.rel_l2(yf, want_f))
+        assert O.rel_l2(yf, fwd_ref) < (5e-6 if prec == 0 else 1e-12), (key, "fwd vs reference")
+        z = torch.empty(p.size_inbox(), dtype=xin.dtype, device="cuda")
+        p.backward(dev(fwd_ref), z, gb.scale.full)
+        zb = host(z)
+        assert O.rel_l2(zb, bwd_ref) < (5e-6 if prec == 0 else 1e-12), (key, "bwd vs reference")
+        assert np.array_equal(host(xin), x)
+
+
+SIZES = [(8, 8, 8), (16, 12, 10), (27, 25, 7), (11, 13, 6), (64, 1, 9), (1, 1, 32), (5, 1, 1), (1, 1, 1),
+         (96, 80, 48), (49, 22, 26), (120, 33, 2)]
+
+
+@pytest.mark.parametrize("size", SIZES)
+@pytest.mark.parametrize("prec", [0, 1])
+def test_c2c_sizes_against_fp64(gb, size, prec):
+    rng = np.random.default_rng(sum(size))
+    n = int(np.prod(size))
+    x = rand_c(rng, n, prec)
+    for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 1, 0), (1, 0, 2))]:
+        y = run_c2c(gb, x, size, io, oo, 0, 0, prec)
+        assert O.rel_l2(y, O.fft3d_c2c(x, size, io, oo)) < TOL[prec], (io, oo)
+        z = run_c2c(gb, y, size, io, oo, 1, 1, prec)
+        assert O.rel_l2(z, O.fft3d_c2c(y, size, oo, io, 1, 1)) < TOL[prec]
+        assert O.rel_l2(z, x) < 3 * TOL[prec]
+
+
+@pytest.mark.parametrize("size", [(10, 9, 8), (7, 6, 5), (16, 16, 16), (2, 3, 4), (33, 10, 1), (128, 20, 12)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_r2c_sizes_against_fp64(gb, size, prec):
+    rng = np.random.default_rng(7 + sum(size))
+    n = int(np.prod(size))
+    x = rng.standard_normal(n).astype(rdt(prec))
+    for rd in range(3):
+        for io, oo in [((0, 1, 2), (0, 1, 2)), ((1, 2, 0), (0, 2, 1))]:
+            for reorder in (0, 1):
+                opts = gb.plan_options.default()
+                opts.use_reorder = reorder
+                ib = gb.box3d((0, 0, 0), [s - 1 for s in size], io)
+                cb = ib.r2c(rd)
+                p = gb.fft3d_r2c(ib, gb.box3d(cb.low, cb.high, oo), rd, opts)
+                xin = dev(x)
+                y = torch.empty(p.size_outbox(), dtype=torch.complex64 if prec == 0 else torch.complex128,
+                                device="cuda")
+                p.forward(xin, y)
+                yh = host(y)
+                assert O.rel_l2(yh, O.fft3d_r2c(x, size, rd, io, oo)) < TOL[prec], (rd, io, oo, reorder)
+                z = torch.empty_like(xin)
+                p.backward(y, z, gb.scale.full)
+                assert O.rel_l2(host(z), x) < 3 * TOL[prec]
+                assert np.array_equal(host(y), yh), "c2r modified its input"
+
+
+@pytest.mark.parametrize("size", [(8, 8, 8), (7, 6, 5), (16, 9, 4), (1, 5, 3), (32, 24, 20)])
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("rkind", [2, 3])
+def test_r2r_sizes_against_fp64(gb, size, prec, rkind):
+    rng = np.random.default_rng(11 + sum(size))
+    n = int(np.prod(size))
+    x = rng.standard_normal(n).astype(rdt(prec))
+    ok = O.COS if rkind == 2 else O.SIN
+    for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 0, 1), (1, 2, 0))]:
+        for reorder in (0, 1):
+            opts = gb.plan_options.default()
+            opts.use_reorder = reorder
+            p = gb.rtransform(rkind, gb.box3d((0, 0, 0), [s - 1 for s in size], io),
+                              gb.box3d((0, 0, 0), [s - 1 for s in size], oo), opts)
+            xin = dev(x)
+            y = torch.empty_like(xin)
+            p.forward(xin, y)
+            assert O.rel_l2(host(y), O.rtransform(ok, x, size, io, oo)) < TOL[prec], (io, oo, reorder)
+            z = torch.empty_like(xin)
+            p.backward(y, z, gb.scale.full)
+            assert O.rel_l2(host(z), O.rtransform(ok, host(y), size, oo, io, 1, 1)) < TOL[prec]
+            assert O.rel_l2(host(z), x) < 3 * TOL[prec]
+
+
+def test_scaling_modes_and_workspace(gb):
+    rng = np.random.default_rng(2)
+    size = (24, 18, 10)
+    x = rand_c(rng, int(np.prod(size)), 1)
+    for sc in (0, 1, 2):
+        for ws in (False, True):
+            y = run_c2c(gb, x, size, (0, 1, 2), (0, 1, 2), 0, sc, 1, workspace=ws)
+            assert O.rel_l2(y, O.fft3d_c2c(x, size, scaling=sc)) < 1e-12
+
+
+def test_in_place_c2c_and_r2c(gb):
+    rng = np.random.default_rng(4)
+    size = (32, 16, 12)
+    n = int(np.prod(size))
+    x = rand_c(rng, n, 0)
+    p = gb.fft3d(gb.box3d((0, 0, 0), (31, 15, 11)), gb.box3d((0, 0, 0), (31, 15, 11)))
+    t = dev(x)
+    p.forward(t, t)
+    assert O.rel_l2(host(t), O.fft3d_c2c(x, size)) < 1e-6
+    # r2c "in place": real input stored in the complex output buffer
+    xr = rng.standard_normal(n).astype(np.float32)
+    pr = gb.fft3d_r2c(gb.box3d((0, 0, 0), (31, 15, 11)), gb.box3d((0, 0, 0), (16, 15, 11)), 0)
+    buf = torch.zeros(pr.size_outbox(), dtype=torch.complex64, device="cuda")
+    buf.view(torch.float32)[:n] = dev(xr)
+    pr.forward(buf.view(torch.float32)[:n], buf)
+    assert O.rel_l2(host(buf), O.fft3d_r2c(xr, size, 0)) < 1e-6
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batch_api(gb, prec):
+    rng = np.random.default_rng(6)
+    size, batch = (12, 10, 9), 5   # test/test_fft3d.h:505-572 uses batch 5 on small boxes
+    n = int(np.prod(size))
+    x = rand_c(rng, n * batch, prec)
+    p = gb.fft3d(gb.box3d((0, 0, 0), (11, 9, 8)), gb.box3d((0, 0, 0), (11, 9, 8)))
+    xin = dev(x)
+    y = torch.empty_like(xin)
+    p.forward_batch(batch, xin, y, gb.scale.symmetric)
+    yh = host(y)
+    for b in range(batch):
+        assert O.rel_l2(yh[b * n:(b + 1) * n], O.fft3d_c2c(x[b * n:(b + 1) * n], size, scaling=2)) < TOL[prec]
+
+
+def test_c2c64_double_configuration(gb, golden):
+    """64^3 complex<double> forward + backward(scale::full) against the reference."""
+    g = golden["c2c64"]
+    rng = np.random.default_rng(64)
+    n = 64 ** 3
+    x = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
+    y = run_c2c(gb, x, (64, 64, 64), (0, 1, 2), (0, 1, 2), 0, 0, 1)
+    assert O.rel_l2(y, O.fft3d_c2c(x, (64, 64, 64))) < 1e-12
+    pos = g["pos"]
+    assert np.abs(y[pos] - g["fwd_sample"]).max() / np.abs(g["fwd_sample"]).max() < 1e-12
+    z = run_c2c(gb, y, (64, 64, 64), (0, 1, 2), (0, 1, 2), 1, 1, 1)
+    assert O.rel_l2(z, x) < 1e-12
+    assert np.abs(z - x).max() < 1e-12
+
+
+def test_errors_on_gpu(gb):
+    p = gb.fft3d(gb.box3d((0, 0, 0), (7, 7, 7)), gb.box3d((0, 0, 0), (7, 7, 7)))
+    a = torch.zeros(512, dtype=torch.complex64, device="cuda")
+    b = torch.zeros(512, dtype=torch.complex128, device="cuda")
+    with pytest.raises(gb.heffte_input_error):
+        p.forward(a, b)
+    with pytest.raises(gb.heffte_input_error):
+        p.forward(a[:100], a)
+    with pytest.raises(gb.heffte_input_error):
+        p.forward(a.cpu(), a)
