@@ -55,6 +55,7 @@ def lib():
     L.heffte_gb300_direct_pack.argtypes = [vp, i, ll, ll, ll, ll, ll, vp, vp]
     L.heffte_gb300_direct_unpack.argtypes = [vp, i, ll, ll, ll, ll, ll, vp, vp]
     L.heffte_gb300_transpose_unpack.argtypes = [vp, i, ll, ll, ll, ll, ll, ll, ll, i, i, i, vp, vp]
+    L.heffte_gb300_r2r_prepost.argtypes = [vp, i, i, i, i, ll, ll, ll, vp, vp]
     L.heffte_gb300_executor_create.argtypes = [i, LL3, LL3, I3, i, I3, ctypes.POINTER(vp)]
     L.heffte_gb300_executor_destroy.argtypes = [vp]
     for f in ("box_size", "complex_size", "workspace_size"):
@@ -327,3 +328,9 @@ def scale_data(prec, num_reals, data, factor, stream=None):
 
 def convert(prec, n, src, dst, to_complex, stream=None):
     check(lib().heffte_gb300_convert(_stream_handle(stream), prec, n, _ptr(src), _ptr(dst), int(to_complex)))
+
+
+def r2r_prepost(prec, rkind, step, length, lines, in_ld, out_ld, src, dst, stream=None):
+    """Batched extended-signal pre/post processing (cos 0, sin 1, cos1 2; steps 0..3)."""
+    check(lib().heffte_gb300_r2r_prepost(_stream_handle(stream), prec, rkind, step, length, lines, in_ld, out_ld,
+                                         _ptr(src), _ptr(dst)))

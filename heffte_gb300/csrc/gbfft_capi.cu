@@ -117,6 +117,20 @@ int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long
     });
 }
 
+int heffte_gb300_r2r_prepost(void *stream, int prec, int kind, int step, int length, long long lines,
+                             long long in_ld, long long out_ld, const void *in, void *out){
+    return guard([&]{
+        check_prec(prec);
+        if (kind < 0 || kind > 2) throw Error(ST_INVALID, "kind must be 0 (cos), 1 (sin) or 2 (cos1)");
+        if (step < 0 || step > 3) throw Error(ST_INVALID, "step must be 0..3");
+        if (length < 1 || (kind == 2 && length < 2) || lines < 0) throw Error(ST_INVALID, "invalid length");
+        if (lines == 0) return;
+        if (!in || !out) throw Error(ST_INVALID, "null pointer");
+        launch_prepost(as_stream(stream), prec, kind, step, length, lines, in_ld, out_ld, in, out);
+        check_cuda(cudaPeekAtLastError(), "r2r pre/post kernel launch");
+    });
+}
+
 // ---------------------------------------------------------------------------
 int heffte_gb300_executor_create(int kind, const long long low[3], const long long high[3], const int order[3],
                                  int ndims, const int dims[3], heffte_gb300_executor *out){

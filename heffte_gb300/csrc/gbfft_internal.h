@@ -77,6 +77,8 @@ void launch_transpose_unpack(cudaStream_t s, int dtype, long long nf, long long 
                              long long ps, long long bls, long long bps, int m0, int m1, void const *src, void *dst);
 void launch_scale(cudaStream_t s, int prec, long long n, void *data, double factor);
 void launch_convert(cudaStream_t s, int prec, long long n, void const *src, void *dst, bool to_complex);
+void launch_prepost(cudaStream_t s, int prec, int kind, int step, int N, long long lines, long long in_ld,
+                    long long out_ld, void const *in, void *out);
 
 // Per-precision kernel launchers (defined in gbfft_fft_f32.cu / _f64.cu).
 struct KernelArgs {

@@ -120,12 +120,13 @@ std::array<int, 3> order_with_first(std::array<int, 3> const &cur, int d){
 std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_box, Box3 const &dst_box,
                           Box3 const &inter_geom, bool reorder, bool out_holds_inter, bool in_aliases_out,
                           int &work_buffers){
-    // drop length-1 passes (identity), keep at least one op to move the data
+    // drop length-1 complex passes (identity), keep at least one op to move
+    // the data; a length-1 r2r transform is not the identity (REDFT10 of one
+    // value is twice the value) and r2c/c2r change the element type
     std::vector<PassSpec> ps;
     for (auto const &p : passes){
-        bool r2x = (p.kind == K_R2C || p.kind == K_C2R);
-        Box3 const &g = (p.kind == K_R2C) ? src_box : inter_geom;
-        if (g.size[p.dim] > 1 || r2x) ps.push_back(p);
+        bool c2c = (p.kind == K_C2C_F || p.kind == K_C2C_B);
+        if (!c2c || inter_geom.size[p.dim] > 1) ps.push_back(p);
     }
     std::vector<Op> ops;
     // logical walk: current box (geometry + order) of the data

@@ -94,6 +94,19 @@ int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long
                                   long long buff_line_stride, long long buff_plane_stride,
                                   int map0, int map1, int map2, const void *src, void *dst);
 
+/* Replaces cuda::{cos,sin,cos1}_pre_pos_processor::{pre,post}_{forward,backward}
+ * (include/heffte_backend_cuda.h:116-174, kernels src/heffte_backend_cuda.cu:149-327)
+ * and batches them: `lines` lines of length `length` (N) in one launch.
+ *   kind: 0 cos (DCT-II/III), 1 sin (DST-II/III), 2 cos1 (DCT-I);
+ *   step: 0 pre_forward  (real N  -> real M),    1 post_forward (complex M/2+1 -> real N),
+ *         2 pre_backward (real N  -> complex M/2+1), 3 post_backward (real M -> real N);
+ *   M = 4N (cos, sin) or 4(N-1) (cos1); in_ld / out_ld: distance between
+ *   lines in elements of the input / output type.  Every output entry of a
+ *   line is written (the reference's pre_forward also zeroes entry 4N, which
+ *   is outside the line and never read). */
+int heffte_gb300_r2r_prepost(void *stream, int prec, int kind, int step, int length, long long lines,
+                             long long in_ld, long long out_ld, const void *in, void *out);
+
 /* ======================================================================= */
 /* 2. Executors (one_dim_backend<tag>::executor / executor_r2c)             */
 /* ======================================================================= */

@@ -343,3 +343,70 @@ def rel_l2(a, b):
     b = np.asarray(b, dtype=a.dtype)
     den = np.linalg.norm(b.ravel())
     return float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))
+
+
+def prepost_line(kind, step, x, N):
+    """One line of cpu_{cos,sin,cos1}_pre_pos_processor (heffte_r2r_executor.h:43-180),
+    restated loop by loop.  step 0 pre_forward, 1 post_forward, 2 pre_backward,
+    3 post_backward.  Returns the output line (pre_forward: the M entries of the
+    extended signal, without the extra entry 4N the reference also zeroes)."""
+    M = 4 * (N - 1) if kind == COS1 else 4 * N
+    if step == 0:
+        sig = np.zeros(M + 1, dtype=x.dtype)
+        if kind == COS:
+            for i in range(N):
+                sig[2 * i] = 0
+                sig[2 * i + 1] = x[i]
+            sig[2 * N] = 0
+            for i in range(2 * N):
+                sig[4 * N - i] = sig[i]
+        elif kind == SIN:
+            for i in range(N):
+                sig[2 * i] = 0
+                sig[2 * i + 1] = x[i]
+            sig[2 * N] = 0
+            for i in range(N):
+                sig[4 * N - 2 * i] = 0
+                sig[4 * N - 2 * i - 1] = -x[i]
+        else:
+            for i in range(N - 1):
+                sig[2 * i] = x[i]
+                sig[2 * i + 1] = 0
+            for i in range(1, N):
+                sig[4 * (N - 1) - 2 * i] = x[i]
+                sig[4 * (N - 1) - 2 * i + 1] = 0
+        return sig[:M]
+    if step == 1:
+        if kind == SIN:
+            return np.array([-x[i + 1].imag for i in range(N)], dtype=x.real.dtype)
+        return np.array([x[i].real for i in range(N)], dtype=x.real.dtype)
+    if step == 2:
+        H = M // 2 + 1
+        cdt = np.complex64 if x.dtype == np.float32 else np.complex128
+        sig = np.zeros(H, dtype=cdt)
+        if kind == COS:
+            for i in range(N):
+                sig[i] = x[i]
+            sig[N] = 0
+            idx = N - 1
+            for i in range(N + 1, 2 * N + 1):
+                sig[i] = -x[idx]
+                idx -= 1
+        elif kind == SIN:
+            sig[0] = 0
+            for i in range(N):
+                sig[i + 1] = -1j * x[i]
+            sig[2 * N] = 0
+            for i in range(N - 1):
+                sig[N + i + 1] = -1j * x[N - i - 2]
+        else:
+            for i in range(N):
+                sig[i] = x[i]
+            idx = N - 2
+            for i in range(N, 2 * N - 1):
+                sig[i] = x[idx]
+                idx -= 1
+        return sig
+    if kind == COS1:
+        return np.array([x[2 * i] for i in range(N)], dtype=x.dtype)
+    return np.array([x[2 * i + 1] for i in range(N)], dtype=x.dtype)

@@ -363,3 +363,24 @@ def test_errors_on_gpu(gb):
         p.forward(a[:100], a)
     with pytest.raises(gb.heffte_input_error):
         p.forward(a.cpu(), a)
+
+
+@pytest.mark.parametrize("rkind", [0, 1, 2])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_r2r_prepost_location_layer_bit_exact(gb, rkind, prec):
+    """Batched pre/post processors against the restated CPU processors (data moves and negations only)."""
+    rng = np.random.default_rng(rkind * 10 + prec)
+    N, lines = 13, 7
+    M = 4 * (N - 1) if rkind == 2 else 4 * N
+    H = M // 2 + 1
+    real = rdt(prec)
+    x = rng.standard_normal(lines * N).astype(real)
+    ext = rng.standard_normal(lines * M).astype(real)
+    cext = rand_c(rng, lines * H, prec)
+    cases = [(0, x, N, M, real), (1, cext, H, N, real), (2, x, N, H, cdt(prec)), (3, ext, M, N, real)]
+    for step, inp, in_ld, out_ld, odt in cases:
+        want = np.concatenate([O.prepost_line(rkind, step, inp[b * in_ld:(b + 1) * in_ld], N)
+                               for b in range(lines)]).astype(odt)
+        out = torch.zeros(lines * out_ld, dtype=torch.from_numpy(np.zeros(1, odt)).dtype, device="cuda")
+        gb.r2r_prepost(prec, rkind, step, N, lines, in_ld, out_ld, dev(inp), out)
+        assert host(out).tobytes() == want.tobytes(), (rkind, step)
