@@ -56,6 +56,8 @@ def lib():
     L.heffte_gb300_direct_unpack.argtypes = [vp, i, ll, ll, ll, ll, ll, vp, vp]
     L.heffte_gb300_transpose_unpack.argtypes = [vp, i, ll, ll, ll, ll, ll, ll, ll, i, i, i, vp, vp]
     L.heffte_gb300_r2r_prepost.argtypes = [vp, i, i, i, i, ll, ll, ll, vp, vp]
+    L.heffte_gb300_set_kernel_variant.argtypes = [i]
+    L.heffte_gb300_device_status.argtypes = [ctypes.POINTER(ctypes.c_int), i]
     L.heffte_gb300_executor_create.argtypes = [i, LL3, LL3, I3, i, I3, ctypes.POINTER(vp)]
     L.heffte_gb300_executor_destroy.argtypes = [vp]
     for f in ("box_size", "complex_size", "workspace_size"):
@@ -334,3 +336,15 @@ def r2r_prepost(prec, rkind, step, length, lines, in_ld, out_ld, src, dst, strea
     """Batched extended-signal pre/post processing (cos 0, sin 1, cos1 2; steps 0..3)."""
     check(lib().heffte_gb300_r2r_prepost(_stream_handle(stream), prec, rkind, step, length, lines, in_ld, out_ld,
                                          _ptr(src), _ptr(dst)))
+
+
+def set_kernel_variant(variant):
+    """0 automatic, 1 generic runtime-radix kernels, 2 pipelined kernels where they apply."""
+    check(lib().heffte_gb300_set_kernel_variant(int(variant)))
+
+
+def device_status(reset=False):
+    """Status word of the current device (0 = no kernel gave up a bounded wait)."""
+    v = ctypes.c_int(-1)
+    check(lib().heffte_gb300_device_status(ctypes.byref(v), int(reset)))
+    return v.value

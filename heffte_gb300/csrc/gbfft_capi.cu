@@ -57,6 +57,22 @@ extern "C" {
 const char *heffte_gb300_last_error(void){ return g_last_error.c_str(); }
 int heffte_gb300_version(void){ return 10000; }
 
+int heffte_gb300_set_kernel_variant(int variant){
+    return guard([&]{
+        if (variant < 0 || variant > 2) throw Error(ST_INVALID, "variant must be 0 (auto), 1 (generic) or 2 (pipelined)");
+        set_kernel_variant(variant);
+    });
+}
+
+int heffte_gb300_device_status(int *status, int reset){
+    return guard([&]{
+        if (!status) throw Error(ST_INVALID, "null pointer");
+        int *d = device_status();
+        check_cuda(cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost), "read device status");
+        if (reset) check_cuda(cudaMemset(d, 0, sizeof(int)), "reset device status");
+    });
+}
+
 int heffte_gb300_convert(void *stream, int prec, long long n, const void *src, void *dst, int to_complex){
     return guard([&]{
         check_prec(prec);

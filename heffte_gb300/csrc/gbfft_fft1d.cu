@@ -1,6 +1,8 @@
 // Host side of one transform length: radix plan, FP64-generated twiddle
 // tables, launch geometry of the batched kernels.
 #include "gbfft_internal.h"
+#include "gbfft_pipe.cuh"
+#include <atomic>
 #include <map>
 #include <math.h>
 
@@ -91,6 +93,9 @@ int max_length(int prec){
 }
 
 std::vector<int> default_radices(int N){
+    // powers of two share the radix plan (and twiddle table) of the pipelined kernels
+    std::vector<int> pr = pipe_radices(N);
+    if (!pr.empty()) return pr;
     std::vector<int> r;
     int n = N;
     for (int p : {13, 11, 7, 5, 3}){
@@ -210,9 +215,53 @@ static void run(cudaStream_t s, int kind, int prec, bool cols, KernelArgs &a){
 
 static bool is_cols(Layout const &Li, Layout const &Lo){ return !(Li.estride == 1 && Lo.estride == 1); }
 
+static std::atomic<int> g_variant{0};
+int kernel_variant(){ return g_variant.load(); }
+void set_kernel_variant(int v){ g_variant.store(v); }
+
+int *device_status(){
+    static int *ptrs[64] = {nullptr};
+    static std::mutex mu;
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    int *&p = ptrs[dev & 63];
+    if (!p){
+        check_cuda(cudaMalloc(&p, sizeof(int)), "cudaMalloc(status word)");
+        check_cuda(cudaMemset(p, 0, sizeof(int)), "cudaMemset(status word)");
+    }
+    return p;
+}
+
+std::vector<int> pipe_radices(int N){
+    if (N < 2 || N > 4096 || (N & (N - 1))) return {};
+    std::vector<int> r;
+    for (int s = 0; s < pipe_nstages(N); s++) r.push_back(pipe_radix(N, s));
+    return r;
+}
+
+// Pipelined path: power-of-two length, not in place across different layouts.
+static bool try_pipe(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout const &Li, Layout const &Lo,
+                     void const *in, void *out, long long G, double scale, LaunchCfg const &cfg){
+    int v = (cfg.variant != 0) ? cfg.variant : kernel_variant();
+    if (v == 1) return false;
+    std::vector<int> pr = pipe_radices(f.N);
+    if (pr.empty() || pr != f.radices) return false;
+    bool same = Li.count == Lo.count && Li.dist == Lo.dist && Li.bstride == Lo.bstride && Li.estride == Lo.estride;
+    if (in == out && !same) return false;
+    bool cols = !(Li.estride == 1 && Lo.estride == 1);
+    PipeArgs a{};
+    a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
+    a.tw = f.twiddles(prec, s);
+    a.G = G; a.scale = scale; a.do_scale = (scale != 1.0);
+    a.status = device_status();
+    return (prec == 0) ? launch_pipe_f32(s, f.N, fwd, cols, a) : launch_pipe_f64(s, f.N, fwd, cols, a);
+}
+
 void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (try_pipe(s, f, prec, fwd, Li, Lo, in, out, G, scale, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, false, G, cfg, a);

@@ -57,7 +57,8 @@ int max_length(int prec);
 
 // Tuning knobs of one launch (chosen by the planner / autotuner).
 struct LaunchCfg {
-    int tpb = 0;   // transforms (or transform pairs) per CTA; 0 = automatic
+    int tpb = 0;      // transforms (or transform pairs) per CTA; 0 = automatic
+    int variant = 0;  // 0 = process-wide choice, 1 = generic kernels, 2 = pipelined kernels
 };
 
 // Batched 1-D launches (in units of elements of the respective arrays).
@@ -100,5 +101,29 @@ struct KernelArgs {
 enum Kind { K_C2C_F, K_C2C_B, K_R2C, K_C2R, K_R2R_F, K_R2R_B };
 void launch_kernel_f32(cudaStream_t s, int kind, bool cols, KernelArgs const &a);
 void launch_kernel_f64(cudaStream_t s, int kind, bool cols, KernelArgs const &a);
+
+// Pipelined power-of-two kernels (gbfft_pipe_f32.cu / _f64.cu); return false
+// when the batch does not meet their tiling / alignment conditions.
+struct PipeArgs {
+    Layout Li, Lo;
+    void const *in;
+    void *out;
+    void const *tw;
+    long long G;
+    double scale;
+    int do_scale;
+    int *status;
+};
+bool launch_pipe_f32(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a);
+bool launch_pipe_f64(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a);
+std::vector<int> pipe_radices(int N);   // empty if N has no pipelined kernel
+
+// Kernel family selection (process-wide): 0 automatic, 1 generic runtime-radix
+// kernels only, 2 pipelined kernels wherever they apply.
+int kernel_variant();
+void set_kernel_variant(int v);
+
+// Per-device status word written by kernels whose bounded waits gave up.
+int *device_status();
 
 } // namespace gbfft

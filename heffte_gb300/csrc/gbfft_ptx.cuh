@@ -1,0 +1,67 @@
+// Inline-PTX helpers for the asynchronous (TMA bulk copy + mbarrier) data
+// path on sm_103a.  Every wait is bounded: it gives up after a clock budget
+// and reports through a device status word instead of spinning forever.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbfft {
+
+// status codes written by kernels into the device status word
+enum { DEV_OK = 0, DEV_TIMEOUT_BULK_COPY = 1 };
+
+__device__ __forceinline__ uint32_t smem_u32(void const *p){
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count){
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// make mbarrier initialisation visible to the async proxy (bulk copies)
+__device__ __forceinline__ void fence_mbar_init(){
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// order this thread's earlier generic-proxy shared-memory accesses before
+// subsequent async-proxy (bulk copy) accesses
+__device__ __forceinline__ void fence_proxy_async_smem(){
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes){
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity){
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of the barrier; gives up after ~`budget` clocks,
+// records DEV_TIMEOUT_BULK_COPY in *status and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status,
+                                                  long long budget = 4000000000LL){
+    if (mbar_try_wait(bar, parity)) return true;
+    long long t0 = clock64();
+    while (true){
+        if (mbar_try_wait(bar, parity)) return true;
+        if (clock64() - t0 > budget){
+            if (status) atomicExch(status, DEV_TIMEOUT_BULK_COPY);
+            return false;
+        }
+    }
+}
+
+// 1-D bulk copy global -> shared completing on an mbarrier (transaction bytes).
+// dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst_smem, void const *src_gmem, uint32_t bytes, uint64_t *bar){
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst_smem)), "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+} // namespace gbfft

@@ -60,6 +60,18 @@ const char *heffte_gb300_last_error(void);
 /* 10000*major + 100*minor + patch */
 int heffte_gb300_version(void);
 
+/* No reference counterpart (tuning / diagnostics of this backend).
+ * Kernel family used by all later calls of this process: 0 automatic
+ * (pipelined power-of-two kernels where they apply), 1 generic runtime-radix
+ * kernels only, 2 pipelined kernels wherever they apply. */
+int heffte_gb300_set_kernel_variant(int variant);
+
+/* No reference counterpart.  Reads the current device's status word (0 = no
+ * fault; 1 = a bounded wait for a bulk copy gave up and the kernel returned
+ * early, its output is invalid).  Synchronises with the device.  reset != 0
+ * clears the word after reading. */
+int heffte_gb300_device_status(int *status, int reset);
+
 /* ======================================================================= */
 /* 1. Location layer                                                        */
 /* ======================================================================= */

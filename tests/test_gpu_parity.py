@@ -384,3 +384,29 @@ def test_r2r_prepost_location_layer_bit_exact(gb, rkind, prec):
         out = torch.zeros(lines * out_ld, dtype=torch.from_numpy(np.zeros(1, odt)).dtype, device="cuda")
         gb.r2r_prepost(prec, rkind, step, N, lines, in_ld, out_ld, dev(inp), out)
         assert host(out).tobytes() == want.tobytes(), (rkind, step)
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_power_of_two_kernel_variants(gb, variant, prec):
+    """Both kernel families (generic runtime-radix, pipelined bulk-copy) on the
+    power-of-two lengths, line and column layouts, in and out of place."""
+    gb.set_kernel_variant(variant)
+    try:
+        rng = np.random.default_rng(variant + 2 * prec)
+        for size in [(2, 4, 8), (16, 32, 64), (128, 16, 32), (256, 8, 16), (512, 16, 32), (32, 1024, 2),
+                     (2048, 2, 16), (4096, 2, 4), (64, 64, 64)]:
+            n = int(np.prod(size))
+            x = rand_c(rng, n, prec)
+            for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 1, 0), (2, 1, 0)), ((1, 0, 2), (0, 2, 1))]:
+                y = run_c2c(gb, x, size, io, oo, 0, 1, prec)
+                assert O.rel_l2(y, O.fft3d_c2c(x, size, io, oo, 0, 1)) < TOL[prec], (size, io, oo)
+                z = run_c2c(gb, y, size, io, oo, 1, 0, prec)
+                assert O.rel_l2(z, x) < 3 * TOL[prec]
+            p = gb.fft3d(gb.box3d((0, 0, 0), [s - 1 for s in size]), gb.box3d((0, 0, 0), [s - 1 for s in size]))
+            t = dev(x)
+            p.forward(t, t)
+            assert O.rel_l2(host(t), O.fft3d_c2c(x, size)) < TOL[prec]
+        assert gb.device_status() == 0
+    finally:
+        gb.set_kernel_variant(0)
