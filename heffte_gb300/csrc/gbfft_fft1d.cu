@@ -233,6 +233,58 @@ int *device_status(){
     return p;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, cuuint64_t const *,
+                                  cuuint64_t const *, cuuint32_t const *, cuuint32_t const *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn(){
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!tried){
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+bool encode_column_tmap(void *tmap, void const *base, int csize, long long count, long long N, long long blocks,
+                        long long estride, long long bstride, int tpb, int boxr, int *swap){
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    long long wpc = csize / 8;
+    bool sw = estride > bstride && blocks > 1;
+    cuuint64_t dims[3], strides[2];
+    cuuint32_t box[3], estr[3] = {1, 1, 1};
+    dims[0] = (cuuint64_t)(count * wpc);
+    box[0] = (cuuint32_t)(tpb * wpc);
+    if (!sw){
+        dims[1] = (cuuint64_t)N; dims[2] = (cuuint64_t)blocks;
+        strides[0] = (cuuint64_t)(estride * csize); strides[1] = (cuuint64_t)(bstride * csize);
+        box[1] = (cuuint32_t)boxr; box[2] = 1;
+    } else {
+        dims[1] = (cuuint64_t)blocks; dims[2] = (cuuint64_t)N;
+        strides[0] = (cuuint64_t)(bstride * csize); strides[1] = (cuuint64_t)(estride * csize);
+        box[1] = 1; box[2] = (cuuint32_t)boxr;
+    }
+    if (blocks == 1) strides[sw ? 0 : 1] = strides[sw ? 1 : 0] * (cuuint64_t)(sw ? N : 1) + 16;
+    CUresult r = fn(reinterpret_cast<CUtensorMap *>(tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(base),
+                    dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    *swap = sw ? 1 : 0;
+    return true;
+}
+
 std::vector<int> pipe_radices(int N){
     if (N < 2 || N > 4096 || (N & (N - 1))) return {};
     std::vector<int> r;

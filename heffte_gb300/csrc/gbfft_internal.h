@@ -114,6 +114,12 @@ struct PipeArgs {
     int do_scale;
     int *status;
 };
+// Tensor map over a batch of column transforms: x = column (8-byte words),
+// then rows and blocks ordered by ascending stride (*swap = 1 when blocks
+// come before rows).  Returns false if the driver rejects the geometry.
+struct CUtensorMap_st;
+bool encode_column_tmap(void *tmap, void const *base, int csize, long long count, long long N, long long blocks,
+                        long long estride, long long bstride, int tpb, int boxr, int *swap);
 bool launch_pipe_f32(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a);
 bool launch_pipe_f64(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a);
 std::vector<int> pipe_radices(int N);   // empty if N has no pipelined kernel

@@ -14,6 +14,7 @@
 //   line tiles (transform along the fastest dimension): TPB contiguous lines,
 //     one bulk copy; the stages exchange through a padded buffer.
 #pragma once
+#include <cuda.h>
 #include "gbfft_common.cuh"
 #include "gbfft_ptx.cuh"
 
@@ -134,10 +135,14 @@ __device__ __forceinline__ long long base_of_fast(Layout const &L, long long g){
     return (g / L.count) * L.bstride + (g % L.count) * L.dist;
 }
 
+// Column tiles are loaded with a 3-D tensor map over the input batch:
+// (x = column in 8-byte words, y = row p of the transform, z = block), box
+// (TPB columns, min(N, 256) rows, 1); one TMA op per 256 rows of a tile.
 template<typename T, int N, bool FWD, bool COLS>
 __global__ void __launch_bounds__(pipe_tpb(N, sizeof(c_t<T>), COLS) * pipe_tt(N))
 k_c2c_pipe(Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
-           long long ntiles, T scale, int do_scale, int *status){
+           long long ntiles, T scale, int do_scale, int *status, const __grid_constant__ CUtensorMap tmap,
+           int tswap){
     using C = c_t<T>;
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
     constexpr int TT = pipe_tt(N);
@@ -158,15 +163,25 @@ k_c2c_pipe(Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> const *__
     }
     __syncthreads();
 
+    if (COLS && tid == 0) prefetch_tmap(&tmap);
     auto issue = [&](long long tile, int b){
-        long long base = base_of_fast(Li, tile * TPB);
         C *dst = tiles + b * TILE;
         if (COLS){
-            if (lane == 0) mbar_arrive_expect_tx(&bar[b], TILE_BYTES);
-            __syncwarp();
-            for (int p = lane; p < N; p += 32)
-                bulk_g2s(dst + p * TPB, in + base + (long long)p * Li.estride, TPB * sizeof(C), &bar[b]);
+            if (lane == 0){
+                constexpr int BOXR = (N < 256) ? N : 256;
+                constexpr int WPC = (int)(sizeof(C) / 8);       // 8-byte words per complex value
+                long long g0 = tile * TPB;
+                int blk = (int)(g0 / Li.count), c0 = (int)(g0 - (long long)blk * Li.count);
+                mbar_arrive_expect_tx(&bar[b], TILE_BYTES);
+                #pragma unroll
+                for (int r0 = 0; r0 < N; r0 += BOXR){
+                    // tswap: the map lists the block dimension before the rows (strides ascending)
+                    if (tswap) tma_load_3d(dst + r0 * TPB, &tmap, c0 * WPC, blk, r0, &bar[b]);
+                    else tma_load_3d(dst + r0 * TPB, &tmap, c0 * WPC, r0, blk, &bar[b]);
+                }
+            }
         } else if (lane == 0){
+            long long base = base_of_fast(Li, tile * TPB);
             mbar_arrive_expect_tx(&bar[b], TILE_BYTES);
             bulk_g2s(dst, in + base, TILE_BYTES, &bar[b]);
         }

@@ -3,6 +3,7 @@
 #include "gbfft_internal.h"
 #include "gbfft_pipe.cuh"
 #include <atomic>
+#include <cstring>
 
 namespace gbfft {
 
@@ -46,8 +47,17 @@ bool run_pipe(cudaStream_t s, PipeArgs const &a){
     long long ntiles = a.G / TPB;
     long long grid = std::min<long long>(ntiles, (long long)num_sms() * blocks_per_sm[dev & 63]);
     if (grid <= 0) return true;
+    CUtensorMap tmap;
+    std::memset(&tmap, 0, sizeof(tmap));
+    int tswap = 0;
+    if (COLS){
+        long long blocks = a.G / a.Li.count;
+        if (!encode_column_tmap(&tmap, a.in, (int)sizeof(C), a.Li.count, N, blocks, a.Li.estride, a.Li.bstride,
+                                TPB, std::min(N, 256), &tswap))
+            return false;
+    }
     kern<<<(unsigned)grid, THREADS, SMEM, s>>>(a.Li, a.Lo, (C const*)a.in, (C*)a.out, (C const*)a.tw, ntiles,
-                                              (T)a.scale, a.do_scale, a.status);
+                                              (T)a.scale, a.do_scale, a.status, tmap, tswap);
     check_cuda(cudaPeekAtLastError(), "pipelined fft kernel launch");
     return true;
 }

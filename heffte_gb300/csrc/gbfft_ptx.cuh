@@ -57,6 +57,19 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     }
 }
 
+// Tiled 3-D tensor copy global -> shared (TMA) completing on an mbarrier.
+// tmap is the address of a CUtensorMap kernel parameter (__grid_constant__).
+// The innermost coordinate times the element size must be a multiple of 16.
+__device__ __forceinline__ void tma_load_3d(void *dst_smem, void const *tmap, int c0, int c1, int c2, uint64_t *bar){
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+                 :: "r"(smem_u32(dst_smem)), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2),
+                    "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(void const *tmap){
+    asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
+}
+
 // 1-D bulk copy global -> shared completing on an mbarrier (transaction bytes).
 // dst, src and bytes must be multiples of 16.
 __device__ __forceinline__ void bulk_g2s(void *dst_smem, void const *src_gmem, uint32_t bytes, uint64_t *bar){
