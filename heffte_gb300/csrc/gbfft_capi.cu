@@ -52,6 +52,10 @@ std::array<int, 3> order_of(int const *o){
 
 } // namespace
 
+namespace gbfft {
+void set_last_error(std::string const &msg){ g_last_error = msg; }
+}
+
 extern "C" {
 
 const char *heffte_gb300_last_error(void){ return g_last_error.c_str(); }

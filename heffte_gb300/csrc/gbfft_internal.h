@@ -28,6 +28,8 @@ inline void check_cuda(cudaError_t e, char const *what){
 
 int num_sms();
 int elem_size(int dtype);
+// message returned by heffte_gb300_last_error() on the calling thread
+void set_last_error(std::string const &msg);
 
 // ---------------------------------------------------------------------------
 // 1-D transform length: radix plan, thread count and device twiddle tables.

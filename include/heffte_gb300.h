@@ -106,6 +106,25 @@ int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long
                                   long long buff_line_stride, long long buff_plane_stride,
                                   int map0, int map1, int map2, const void *src, void *dst);
 
+/* No counterpart in the reference.  transpose_unpack performed in place, for
+ * callers that cannot allocate device memory: programs whose device memory is
+ * owned by an arena that forbids other allocations, real-time loops that must
+ * not allocate after start-up (cudaMalloc can synchronise the device and take
+ * unbounded time), and callers at the memory limit.  `data` holds the source
+ * in the buffer layout (buff_line_stride, buff_plane_stride) and receives the
+ * destination (line_stride, plane_stride); the six maps are those of
+ * heffte_gb300_transpose_unpack.  The source is staged in a fixed 32 MiB
+ * scratch array inside the library (reserved on every GPU that loads the
+ * library until the process exits); a larger source is rejected with
+ * HEFFTE_GB300_INVALID.  The first call on a device looks up the array's
+ * device address; make it before any stream capture.  All calls share the
+ * array, which keeps the last call's contents, so calls that overlap on the
+ * GPU (e.g. on two streams) race.  Nothing is allocated. */
+int heffte_gb300_transpose_unpack_inplace_noalloc(void *stream, int dtype, long long nfast, long long nmid,
+                                                  long long nslow, long long line_stride, long long plane_stride,
+                                                  long long buff_line_stride, long long buff_plane_stride,
+                                                  int map0, int map1, int map2, void *data);
+
 /* Replaces cuda::{cos,sin,cos1}_pre_pos_processor::{pre,post}_{forward,backward}
  * (include/heffte_backend_cuda.h:116-174, kernels src/heffte_backend_cuda.cu:149-327)
  * and batches them: `lines` lines of length `length` (N) in one launch.
