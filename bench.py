@@ -37,6 +37,7 @@ def parse():
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--prec", default="single", choices=["single", "double"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="", help="report other configurations: a name, a comma list or 'all'")
     return ap.parse_args()
 
 
@@ -300,8 +301,87 @@ def ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+WORKLOADS = {
+    # name: (kind, size, precision) — the other configurations of the metric's
+    # table, reported by --workload (parity cases; not the contract line)
+    "c2c512": ("c2c", (512, 512, 512), 0),
+    "r2c512": ("r2c", (512, 512, 512), 0),
+    "dct256": ("cos", (256, 256, 256), 0),
+    "z2z512": ("c2c", (512, 512, 512), 1),
+    "c2c1024x1024x512": ("c2c", (1024, 1024, 512), 0),
+    "z2z64": ("c2c", (64, 64, 64), 1),
+}
+
+
+def algorithmic_bytes(kind, size, prec):
+    """Bytes of the three passes of one transform (read + write per pass)."""
+    N = size[0] * size[1] * size[2]
+    rs, cs = (4, 8) if prec == 0 else (8, 16)
+    if kind == "c2c":
+        return 3 * 2 * N * cs
+    if kind == "r2c":
+        nc = (size[0] // 2 + 1) * size[1] * size[2]
+        return N * rs + nc * cs + 4 * nc * cs
+    return 3 * 2 * N * rs
+
+
+def run_workload(name, steps, warmup):
+    import torch
+    import heffte_gb300 as gb
+    kind, size, prec = WORKLOADS[name]
+    N = size[0] * size[1] * size[2]
+    stream = torch.cuda.current_stream()
+    box = gb.box3d((0, 0, 0), [s - 1 for s in size])
+    rdt = torch.float32 if prec == 0 else torch.float64
+    cdt = torch.complex64 if prec == 0 else torch.complex128
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(99)
+    if kind == "c2c":
+        plan = gb.fft3d(box, box, stream=stream)
+        x = torch.complex(torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1,
+                          torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1)
+        y, z = torch.empty_like(x), torch.empty_like(x)
+        wdt = cdt
+    elif kind == "r2c":
+        plan = gb.fft3d_r2c(box, box.r2c(0), 0, stream=stream)
+        x = torch.randn(N, device="cuda", generator=gen, dtype=rdt)
+        y = torch.empty(plan.size_outbox(), device="cuda", dtype=cdt)
+        z = torch.empty_like(x)
+        wdt = cdt
+    else:
+        plan = gb.rtransform(gb.kind.cos, box, box, stream=stream)
+        x = torch.randn(N, device="cuda", generator=gen, dtype=rdt)
+        y, z = torch.empty_like(x), torch.empty_like(x)
+        wdt = rdt
+    work = torch.empty(max(plan.size_workspace(), 1), dtype=wdt, device="cuda")
+
+    def step():
+        plan.forward_buffered(x, y, work, gb.scale.full)
+        plan.backward_buffered(y, z, work, gb.scale.none)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    err = float((z - x).abs().max().item())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    b = 2 * algorithmic_bytes(kind, size, prec)
+    peak, _ = peaks()
+    return {"workload": name, "ms_per_step": ms, "gflops": 2 * flops_per_transform(N) / (ms / 1e3) / 1e9,
+            "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak, "roundtrip_max_abs": err}
+
+
 def main():
     args = parse()
+    if args.workload:
+        for name in (WORKLOADS if args.workload == "all" else args.workload.split(",")):
+            print(json.dumps(run_workload(name, args.steps, args.warmup)), flush=True)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
