@@ -257,11 +257,14 @@ static EncodeTiledFn encode_fn(){
     return fn;
 }
 
-bool encode_column_tmap(void *tmap, void const *base, int csize, long long count, long long N, long long blocks,
-                        long long estride, long long bstride, int tpb, int boxr, int *swap){
+bool encode_column_tmap(void *tmap, void const *base, int esize, long long count, long long N, long long blocks,
+                        long long estride, long long bstride, int width, int boxr, int *swap){
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
-    long long wpc = csize / 8;
+    // 4-byte elements map to FLOAT32 words, 8- and 16-byte elements to FLOAT64 words
+    long long wpc = (esize >= 8) ? esize / 8 : 1;
+    int csize = esize;
+    int tpb = width;
     bool sw = estride > bstride && blocks > 1;
     cuuint64_t dims[3], strides[2];
     cuuint32_t box[3], estr[3] = {1, 1, 1};
@@ -277,7 +280,8 @@ bool encode_column_tmap(void *tmap, void const *base, int csize, long long count
         box[1] = 1; box[2] = (cuuint32_t)boxr;
     }
     if (blocks == 1) strides[sw ? 0 : 1] = strides[sw ? 1 : 0] * (cuuint64_t)(sw ? N : 1) + 16;
-    CUresult r = fn(reinterpret_cast<CUtensorMap *>(tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(base),
+    CUtensorMapDataType dt = (esize == 4) ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    CUresult r = fn(reinterpret_cast<CUtensorMap *>(tmap), dt, 3, const_cast<void *>(base),
                     dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return false;
@@ -293,27 +297,49 @@ std::vector<int> pipe_radices(int N){
 }
 
 // Pipelined path: power-of-two length, not in place across different layouts.
-static bool try_pipe(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout const &Li, Layout const &Lo,
-                     void const *in, void *out, long long G, double scale, LaunchCfg const &cfg){
+// Merges the two batch levels of a layout when its blocks are contiguous
+// (bstride = count * dist), so that column tiles can span whole planes.
+static void merge_blocks(Layout &Li, Layout &Lo, long long G){
+    if (Li.bstride == Li.count * Li.dist && Lo.bstride == Lo.count * Lo.dist && Li.count == Lo.count){
+        Li.count = G; Li.bstride = G * Li.dist;
+        Lo.count = G; Lo.bstride = G * Lo.dist;
+    }
+}
+
+// Pipelined path: power-of-two length, not in place across different layouts
+// (the element type changes for r2c/c2r: never in place).
+static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
+                     long long G, double scale, int sine, LaunchCfg const &cfg){
     int v = (cfg.variant != 0) ? cfg.variant : kernel_variant();
     if (v == 1) return false;
     std::vector<int> pr = pipe_radices(f.N);
-    if (pr.empty() || pr != f.radices) return false;
+    if (pr.empty() || pr != f.radices || f.N < 16) return false;
     bool same = Li.count == Lo.count && Li.dist == Lo.dist && Li.bstride == Lo.bstride && Li.estride == Lo.estride;
-    if (in == out && !same) return false;
+    if (in == out && (!same || kind == K_R2C || kind == K_C2R)) return false;
     bool cols = !(Li.estride == 1 && Lo.estride == 1);
-    PipeArgs a{};
+    if (!cols && (Li.estride != 1)) return false;
+    merge_blocks(Li, Lo, G);
+    PipeLaunch a{};
     a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
     a.tw = f.twiddles(prec, s);
-    a.G = G; a.scale = scale; a.do_scale = (scale != 1.0);
+    a.rtw = (kind == K_R2R_F || kind == K_R2R_B) ? f.r2r_twiddles(prec, s) : nullptr;
+    a.G = G; a.scale = scale; a.sine = sine;
     a.status = device_status();
-    return (prec == 0) ? launch_pipe_f32(s, f.N, fwd, cols, a) : launch_pipe_f64(s, f.N, fwd, cols, a);
+    bool c2c = (kind == K_C2C_F || kind == K_C2C_B), r2c = (kind == K_R2C || kind == K_C2R);
+    if (prec == 0){
+        if (c2c) return launch_pipe_f32_c2c(s, kind, f.N, cols, a);
+        if (r2c) return launch_pipe_f32_r2c(s, kind, f.N, cols, a);
+        return launch_pipe_f32_r2r(s, kind, f.N, cols, a);
+    }
+    if (c2c) return launch_pipe_f64_c2c(s, kind, f.N, cols, a);
+    if (r2c) return launch_pipe_f64_r2c(s, kind, f.N, cols, a);
+    return launch_pipe_f64_r2r(s, kind, f.N, cols, a);
 }
 
 void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
-    if (try_pipe(s, f, prec, fwd, Li, Lo, in, out, G, scale, cfg)) return;
+    if (try_pipe(s, fwd ? K_C2C_F : K_C2C_B, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, false, G, cfg, a);
@@ -326,6 +352,7 @@ void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout 
 void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (try_pipe(s, K_R2C, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, true, G, cfg, a);
@@ -338,6 +365,7 @@ void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void c
 void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (try_pipe(s, K_C2R, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, true, G, cfg, a);
@@ -350,6 +378,7 @@ void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void c
 void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout Li, Layout Lo, void const *in,
                 void *out, long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (try_pipe(s, fwd ? K_R2R_F : K_R2R_B, f, prec, Li, Lo, in, out, G, scale, sine ? 1 : 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, true, G, cfg, a);

@@ -106,24 +106,30 @@ void launch_kernel_f64(cudaStream_t s, int kind, bool cols, KernelArgs const &a)
 
 // Pipelined power-of-two kernels (gbfft_pipe_f32.cu / _f64.cu); return false
 // when the batch does not meet their tiling / alignment conditions.
-struct PipeArgs {
+struct PipeLaunch {
     Layout Li, Lo;
     void const *in;
     void *out;
     void const *tw;
+    void const *rtw;
     long long G;
     double scale;
-    int do_scale;
+    int sine;
     int *status;
 };
+// one dispatcher per precision and kind group (c2c / r2c+c2r / r2r), kind = K_*
+bool launch_pipe_f32_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+bool launch_pipe_f32_r2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+bool launch_pipe_f32_r2r(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+bool launch_pipe_f64_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+bool launch_pipe_f64_r2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+bool launch_pipe_f64_r2r(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 // Tensor map over a batch of column transforms: x = column (8-byte words),
 // then rows and blocks ordered by ascending stride (*swap = 1 when blocks
 // come before rows).  Returns false if the driver rejects the geometry.
 struct CUtensorMap_st;
 bool encode_column_tmap(void *tmap, void const *base, int csize, long long count, long long N, long long blocks,
                         long long estride, long long bstride, int tpb, int boxr, int *swap);
-bool launch_pipe_f32(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a);
-bool launch_pipe_f64(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a);
 std::vector<int> pipe_radices(int N);   // empty if N has no pipelined kernel
 
 // Kernel family selection (process-wide): 0 automatic, 1 generic runtime-radix

@@ -1,24 +1,32 @@
 // Pipelined batched transforms for power-of-two lengths (sm_103a).
 //
-// Persistent CTAs walk over tiles of TPB transforms.  Each tile is streamed
-// from HBM into shared memory by 1-D bulk copies (the TMA engine) that
-// complete on an mbarrier, double-buffered: while the CTA transforms tile i,
-// tile i+1 is already in flight.  Transform length, radix sequence and tile
-// shape are compile-time constants, so index arithmetic folds to shifts and
-// the butterflies are straight-line code; the result leaves the registers of
-// the last radix stage directly for HBM.
-//
-//   column tiles (transform along a strided dimension): TPB adjacent columns
-//     x N rows; row p of the tile is one bulk copy of TPB*sizeof(C) bytes;
-//     the radix stages exchange through the tile buffer itself.
-//   line tiles (transform along the fastest dimension): TPB contiguous lines,
-//     one bulk copy; the stages exchange through a padded buffer.
+// Persistent CTAs walk over tiles of TPB "units" (one complex transform, or a
+// pair of real transforms packed into one complex FFT).  Each tile is
+// streamed from HBM into shared memory while the previous tile is being
+// transformed (double buffering), by one of three loaders:
+//   TENSOR  column tiles through a 3-D TMA tensor map (x = column, rows,
+//           blocks), one TMA op per 256 rows; out-of-range columns are filled
+//           with zeros by the TMA unit;
+//   BULK    line tiles (transform along the fastest dimension, lines
+//           contiguous) as one 1-D bulk copy;
+//   CPASYNC column tiles element by element with cp.async (any alignment,
+//           e.g. the odd row stride of an r2c half-spectrum box).
+// TMA copies complete on mbarriers whose waits are bounded (a device status
+// word reports a wait that gave up); cp.async copies complete on commit
+// groups.  Transform length, radix plan and tile shape are compile-time
+// constants; the radix-stage exchange happens in shared memory and the last
+// stage (or the fused post-processing of r2c / DCT) stores straight to HBM.
 #pragma once
 #include <cuda.h>
 #include "gbfft_common.cuh"
 #include "gbfft_ptx.cuh"
 
 namespace gbfft {
+
+// kinds (same numbering as the host-side kernel kinds)
+enum { PK_C2C_FWD = 0, PK_C2C_BWD = 1, PK_R2C_FWD = 2, PK_C2R_BWD = 3, PK_R2R_FWD = 4, PK_R2R_BWD = 5 };
+// loaders
+enum { LD_TENSOR = 0, LD_BULK = 1, LD_CPASYNC = 2 };
 
 // Radix plan of the pipelined kernels: at most 16 values per thread.
 __host__ __device__ constexpr int pipe_nstages(int N){
@@ -57,46 +65,70 @@ __host__ __device__ constexpr int cilog2(int v){
     return l;
 }
 __host__ __device__ constexpr int pipe_pe(int N){ return (N < 16) ? N : 16; }     // values per thread
-__host__ __device__ constexpr int pipe_tt(int N){ return N / pipe_pe(N); }        // threads per transform
+__host__ __device__ constexpr int pipe_tt(int N){ return N / pipe_pe(N); }        // threads per unit
 __host__ __device__ constexpr int pipe_padn(int N){ return N + N / 16 + 1; }
-// transforms per tile
+__host__ __device__ constexpr bool pipe_paired(int kind){ return kind >= PK_R2C_FWD; }
+// units (complex transforms or real pairs) per tile
 __host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols){
     int tt = pipe_tt(N);
     int tpb = cols ? ((csize == 8) ? 16 : 8) : 1;
     if (cols){ while (tpb * tt < 256 && tpb < 256) tpb *= 2; }
     else { while (tpb * tt < 256) tpb *= 2; }
     while (tpb > 1 && tpb * tt > 512) tpb /= 2;
-    while (tpb > 1 && 2 * N * tpb * csize > 160 * 1024) tpb /= 2;
+    while (tpb > 1 && 2 * (N + 2) * tpb * csize > 160 * 1024) tpb /= 2;
     return tpb;
 }
-__host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols){
+// complex elements of one tile buffer (the c2r input tile holds N/2+1 rows of 2*TPB values)
+__host__ __device__ constexpr int pipe_tile_elems(int N, int tpb, int kind){
+    return (kind == PK_C2R_BWD) ? (N / 2 + 1) * 2 * tpb : N * tpb;
+}
+__host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind){
     int tpb = pipe_tpb(N, csize, cols);
-    return 2 * N * tpb * csize + (cols ? 0 : tpb * pipe_padn(N) * csize);
+    return 2 * pipe_tile_elems(N, tpb, kind) * csize + (cols ? 0 : tpb * pipe_padn(N) * csize);
 }
 
-template<typename T, int N, int TPB, int S, bool FWD, bool COLS, class ST>
-__device__ __forceinline__ void pipe_stage(int t, int loc, c_t<T> *tile, c_t<T> *xch, c_t<T> const *__restrict__ tw,
-                                           c_t<T> (&v)[16], ST &st){
+struct PipeParams {
+    Layout Li, Lo;          // per transform (real or complex elements of each array)
+    void const *in;
+    void *out;
+    void const *tw;         // Stockham twiddles
+    void const *rtw;        // exp(-i pi k / 2N) (r2r)
+    long long G;            // transforms
+    long long ntiles;
+    long long tiles_per_block;  // column tiles: tiles covering one block of `count` columns
+    double scale;
+    int do_scale;
+    int sine;
+    int tswap;
+    int *status;
+};
+
+// One radix stage; S == 0 reads through ld0, the last stage writes through st
+// (or to the exchange buffer when POST is set).
+template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST, class LD, class ST>
+__device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const *__restrict__ tw,
+                                       c_t<T> (&v)[16], LD &ld0, ST &st){
     using C = c_t<T>;
     constexpr int NS = pipe_nstages(N);
     if constexpr (S < NS){
         constexpr int R = pipe_radix(N, S), Ns = pipe_ns(N, S), TWO = pipe_twoff(N, S);
         constexpr int NR = N / R, TT = pipe_tt(N), M = pipe_pe(N) / R, PADN = pipe_padn(N);
         constexpr bool LAST = (S == NS - 1);
+        constexpr bool TO_XCH = !LAST || POST;
         constexpr int LNS = cilog2(Ns), LNSR = cilog2(Ns * R);
-        C const *src = (COLS || S == 0) ? tile : xch;
+        auto xi = [&](int p) -> int { return COLS ? (p * TPB + loc) : (loc * PADN + p + (p >> 4)); };
         #pragma unroll
         for (int m = 0; m < M; m++){
             int j = t + m * TT;
             #pragma unroll
             for (int q = 0; q < R; q++){
                 int p = j + q * NR;
-                int ix = COLS ? (p * TPB + loc) : ((S == 0) ? (loc * N + p) : (loc * PADN + p + (p >> 4)));
-                v[m * R + q] = src[ix];
+                if constexpr (S == 0) v[m * R + q] = ld0(p);
+                else v[m * R + q] = xch[xi(p)];
             }
         }
-        // the next writes go to the buffer just read (column tiles, later stages)
-        if (!LAST && (COLS || S > 0)) __syncthreads();
+        // the exchange buffer is rewritten below: everyone must have read it
+        if (TO_XCH) __syncthreads();
         #pragma unroll
         for (int m = 0; m < M; m++){
             int j = t + m * TT;
@@ -114,15 +146,12 @@ __device__ __forceinline__ void pipe_stage(int t, int loc, c_t<T> *tile, c_t<T> 
             #pragma unroll
             for (int q = 0; q < R; q++){
                 int p = ob + q * Ns;
-                if constexpr (LAST) st(p, v[m * R + q]);
-                else {
-                    int ix = COLS ? (p * TPB + loc) : (loc * PADN + p + (p >> 4));
-                    (COLS ? tile : xch)[ix] = v[m * R + q];
-                }
+                if constexpr (TO_XCH) xch[xi(p)] = v[m * R + q];
+                else st(p, v[m * R + q]);
             }
         }
-        if (!LAST) __syncthreads();
-        pipe_stage<T, N, TPB, S + 1, FWD, COLS>(t, loc, tile, xch, tw, v, st);
+        if (TO_XCH) __syncthreads();
+        pstage<T, N, TPB, S + 1, FWD, COLS, POST>(t, loc, xch, tw, v, ld0, st);
     }
 }
 
@@ -135,80 +164,260 @@ __device__ __forceinline__ long long base_of_fast(Layout const &L, long long g){
     return (g / L.count) * L.bstride + (g % L.count) * L.dist;
 }
 
-// Column tiles are loaded with a 3-D tensor map over the input batch:
-// (x = column in 8-byte words, y = row p of the transform, z = block), box
-// (TPB columns, min(N, 256) rows, 1); one TMA op per 256 rows of a tile.
-template<typename T, int N, bool FWD, bool COLS>
-__global__ void __launch_bounds__(pipe_tpb(N, sizeof(c_t<T>), COLS) * pipe_tt(N))
-k_c2c_pipe(Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
-           long long ntiles, T scale, int do_scale, int *status, const __grid_constant__ CUtensorMap tmap,
-           int tswap){
+__device__ __forceinline__ void cp_async_8(void *dst, void const *src, bool valid){
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(smem_u32(dst)), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_16(void *dst, void const *src, bool valid){
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" :: "r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit(){ asm volatile("cp.async.commit_group;" ::: "memory"); }
+template<int NG> __device__ __forceinline__ void cp_async_wait(){ asm volatile("cp.async.wait_group %0;" :: "n"(NG) : "memory"); }
+
+__host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols){ return pipe_tpb(N, csize, cols) * pipe_tt(N); }
+
+template<typename T, int N, int KIND, bool COLS, int LOADER>
+__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS))
+k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
+    constexpr bool PAIRED = pipe_paired(KIND);
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
     constexpr int TT = pipe_tt(N);
-    constexpr int TILE = N * TPB;
-    constexpr uint32_t TILE_BYTES = (uint32_t)(TILE * sizeof(C));
+    constexpr int NT = TPB * TT;
+    constexpr int TILE = pipe_tile_elems(N, TPB, KIND);   // complex elements per buffer
+    constexpr int H = N / 2 + 1;
+    // input of one tile: rows x width (columns) or lines x line_len, in input elements
+    constexpr int IN_ES = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) ? (int)sizeof(T) : (int)sizeof(C);
+    constexpr int ROWS = (KIND == PK_C2R_BWD) ? H : N;
+    constexpr int WIDTH = PAIRED ? 2 * TPB : TPB;           // input elements per tile row (columns)
+    constexpr int LINE_LEN = (KIND == PK_C2R_BWD) ? H : N;  // input elements per line
+    constexpr bool FWD = (KIND == PK_C2C_FWD || KIND == PK_R2C_FWD || KIND == PK_R2R_FWD);
+    constexpr int PADN = pipe_padn(N);
+
     extern __shared__ __align__(128) unsigned char smraw[];
     C *tiles = reinterpret_cast<C*>(smraw);
-    C *xch = tiles + 2 * TILE;
+    C *xline = tiles + 2 * TILE;     // line tiles: padded exchange buffer
     __shared__ __align__(8) uint64_t bar[2];
+
     int tid = threadIdx.x;
     int loc, t;
     if (COLS){ loc = tid % TPB; t = tid / TPB; } else { loc = tid / TT; t = tid % TT; }
-    int warp = tid >> 5, lane = tid & 31;
-    if (tid == 0){
+    int lane = tid & 31, warp = tid >> 5;
+    Layout const Li = P.Li, Lo = P.Lo;
+    int units_per = PAIRED ? 2 : 1;
+
+    if (LOADER != LD_CPASYNC && tid == 0){
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
     }
+    if (LOADER == LD_TENSOR && tid == 0) prefetch_tmap(&tmap);
     __syncthreads();
 
-    if (COLS && tid == 0) prefetch_tmap(&tmap);
-    auto issue = [&](long long tile, int b){
-        C *dst = tiles + b * TILE;
+    // tile -> (block, first column) for column tiles, first line for line tiles
+    auto tile_origin = [&](long long tile, long long &blk, long long &c0){
         if (COLS){
-            if (lane == 0){
-                constexpr int BOXR = (N < 256) ? N : 256;
-                constexpr int WPC = (int)(sizeof(C) / 8);       // 8-byte words per complex value
-                long long g0 = tile * TPB;
-                int blk = (int)(g0 / Li.count), c0 = (int)(g0 - (long long)blk * Li.count);
-                mbar_arrive_expect_tx(&bar[b], TILE_BYTES);
-                #pragma unroll
-                for (int r0 = 0; r0 < N; r0 += BOXR){
-                    // tswap: the map lists the block dimension before the rows (strides ascending)
-                    if (tswap) tma_load_3d(dst + r0 * TPB, &tmap, c0 * WPC, blk, r0, &bar[b]);
-                    else tma_load_3d(dst + r0 * TPB, &tmap, c0 * WPC, r0, blk, &bar[b]);
-                }
-            }
-        } else if (lane == 0){
-            long long base = base_of_fast(Li, tile * TPB);
-            mbar_arrive_expect_tx(&bar[b], TILE_BYTES);
-            bulk_g2s(dst, in + base, TILE_BYTES, &bar[b]);
+            blk = tile / P.tiles_per_block;
+            c0 = (tile - blk * P.tiles_per_block) * WIDTH;
+        } else {
+            blk = 0;
+            c0 = tile * (long long)TPB * units_per;   // first line
         }
     };
 
-    uint32_t phase0 = 0, phase1 = 0;
+    auto issue = [&](long long tile, int b){
+        long long blk, c0;
+        tile_origin(tile, blk, c0);
+        unsigned char *dst = reinterpret_cast<unsigned char*>(tiles + b * TILE);
+        if constexpr (LOADER == LD_TENSOR){
+            if (warp == 0 && lane == 0){
+                constexpr int BOXR = (ROWS < 256) ? ROWS : 256;
+                constexpr int WPE = (IN_ES >= 8) ? IN_ES / 8 : 1;      // tensor words per input element
+                mbar_arrive_expect_tx(&bar[b], (uint32_t)(ROWS * WIDTH * IN_ES));
+                #pragma unroll
+                for (int r0 = 0; r0 < ROWS; r0 += BOXR){
+                    int x = (int)(c0 * WPE);
+                    if (P.tswap) tma_load_3d(dst + (size_t)r0 * WIDTH * IN_ES, &tmap, x, (int)blk, r0, &bar[b]);
+                    else tma_load_3d(dst + (size_t)r0 * WIDTH * IN_ES, &tmap, x, r0, (int)blk, &bar[b]);
+                }
+            }
+        } else if constexpr (LOADER == LD_BULK){
+            if (warp == 0 && lane == 0){
+                long long lines = ((long long)TPB * units_per < P.G - c0) ? (long long)TPB * units_per : (P.G - c0);
+                uint32_t bytes = (uint32_t)(lines * LINE_LEN * IN_ES);
+                long long base = base_of_fast(Li, c0);
+                mbar_arrive_expect_tx(&bar[b], bytes);
+                bulk_g2s(dst, reinterpret_cast<unsigned char const*>(P.in) + base * IN_ES, bytes, &bar[b]);
+            }
+        } else {
+            // cp.async, element by element (8- or 16-byte elements), zero fill out
+            // of range; each thread keeps one column (NT is a multiple of WIDTH)
+            long long rstride = Li.estride * IN_ES;
+            if constexpr (NT % WIDTH == 0){
+                constexpr int RSTEP = NT / WIDTH;
+                int c = tid % WIDTH, r = tid / WIDTH;
+                bool valid = (c0 + c) < Li.count;
+                long long col = valid ? base_of_fast(Li, blk * Li.count + c0 + c) : 0;
+                unsigned char const *src = reinterpret_cast<unsigned char const*>(P.in) + col * IN_ES;
+                #pragma unroll 4
+                for (; r < ROWS; r += RSTEP){
+                    int e = r * WIDTH + c;
+                    if constexpr (IN_ES == 16) cp_async_16(dst + (size_t)e * 16, src + (valid ? r * rstride : 0), valid);
+                    else cp_async_8(dst + (size_t)e * 8, src + (valid ? r * rstride : 0), valid);
+                }
+            } else {
+                for (int e = tid; e < ROWS * WIDTH; e += NT){
+                    int r = e / WIDTH, c = e - r * WIDTH;
+                    bool valid = (c0 + c) < Li.count;
+                    long long off = valid ? base_of_fast(Li, blk * Li.count + c0 + c) * IN_ES + r * rstride : 0;
+                    unsigned char const *src = reinterpret_cast<unsigned char const*>(P.in) + off;
+                    if constexpr (IN_ES == 16) cp_async_16(dst + (size_t)e * 16, src, valid);
+                    else cp_async_8(dst + (size_t)e * 8, src, valid);
+                }
+            }
+            cp_async_commit();
+        }
+    };
+
+    uint32_t ph0 = 0, ph1 = 0;
     long long tile = blockIdx.x;
-    if (tile < ntiles && warp == 0) issue(tile, 0);
-    for (int it = 0; tile < ntiles; tile += gridDim.x, it++){
+    if (tile < P.ntiles) issue(tile, 0);
+    T sc = (T)P.scale;
+    for (int it = 0; tile < P.ntiles; tile += gridDim.x, it++){
         int b = it & 1;
         long long nxt = tile + gridDim.x;
-        if (nxt < ntiles && warp == 0){
-            // the buffer was last read in the previous iteration (ended by a barrier)
-            fence_proxy_async_smem();
+        if (nxt < P.ntiles){
+            if (LOADER != LD_CPASYNC && warp == 0) fence_proxy_async_smem();
             issue(nxt, b ^ 1);
         }
-        uint32_t ph = b ? phase1 : phase0;
-        // every wait is bounded; if any thread gave up, the whole CTA leaves
-        bool ok = mbar_wait_bounded(&bar[b], ph, status);
-        if (__syncthreads_or(!ok)) return;
-        if (b) phase1 ^= 1; else phase0 ^= 1;
+        if constexpr (LOADER == LD_CPASYNC){
+            if (nxt < P.ntiles) cp_async_wait<1>(); else cp_async_wait<0>();
+            __syncthreads();
+        } else {
+            bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0, P.status);
+            if (__syncthreads_or(!ok)) return;
+            if (b) ph1 ^= 1; else ph0 ^= 1;
+        }
 
-        long long ob = base_of_fast(Lo, tile * TPB + loc);
+        C *tb = tiles + b * TILE;
+        C *xch = COLS ? tb : xline;
+        long long blk, c0;
+        tile_origin(tile, blk, c0);
+        // transforms of this thread's unit
+        long long ga, gb;
+        bool va, vb;
+        if (COLS){
+            long long ca = c0 + (long long)loc * units_per;
+            va = ca < Li.count;
+            vb = PAIRED ? (ca + 1 < Li.count) : false;
+            ga = blk * Li.count + ca;
+            gb = ga + 1;
+        } else {
+            ga = c0 + (long long)loc * units_per;
+            gb = ga + 1;
+            va = ga < P.G;
+            vb = PAIRED ? (gb < P.G) : false;
+        }
+        long long oa = va ? base_of_fast(Lo, ga) : 0, obb = vb ? base_of_fast(Lo, gb) : 0;
         long long oes = Lo.estride;
-        auto st = [&](int p, C v){ out[ob + p * oes] = do_scale ? cscale(v, scale) : v; };
+        T const *tr = reinterpret_cast<T const*>(tb);
+        int sine = P.sine;
         C v[16];
-        pipe_stage<T, N, TPB, 0, FWD, COLS>(t, loc, tiles + b * TILE, xch, tw, v, st);
+
+        if constexpr (KIND == PK_C2C_FWD || KIND == PK_C2C_BWD){
+            auto ld0 = [&](int p) -> C { return COLS ? tb[p * TPB + loc] : tb[loc * N + p]; };
+            C *out = reinterpret_cast<C*>(P.out);
+            auto st = [&](int p, C x){ if (va) out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
+            pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+        } else if constexpr (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD){
+            auto ld0 = [&](int p) -> C {
+                int n = p;
+                T sg = (T)1;
+                if constexpr (KIND == PK_R2R_FWD){
+                    n = (2 * p < N) ? 2 * p : 2 * (N - 1 - p) + 1;   // Makhoul reordering
+                    if (sine && (n & 1)) sg = (T)-1;
+                }
+                C z;
+                if (COLS){ z = tb[n * TPB + loc]; }
+                else { z.x = tr[(2 * loc) * N + n]; z.y = tr[(2 * loc + 1) * N + n]; }
+                z.x *= sg; z.y *= sg;
+                return z;
+            };
+            auto st = [&](int, C){};
+            pstage<T, N, TPB, 0, true, COLS, true>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            auto xi = [&](int p) -> int { return COLS ? (p * TPB + loc) : (loc * PADN + p + (p >> 4)); };
+            if constexpr (KIND == PK_R2C_FWD){
+                C *out = reinterpret_cast<C*>(P.out);
+                T h = (T)0.5 * (P.do_scale ? sc : (T)1);
+                for (int k = t; k <= N / 2; k += TT){
+                    C zk = xch[xi(k)], zn = xch[xi((k == 0) ? 0 : N - k)];
+                    C xa; xa.x = h * (zk.x + zn.x); xa.y = h * (zk.y - zn.y);
+                    C xb; xb.x = h * (zk.y + zn.y); xb.y = -h * (zk.x - zn.x);
+                    if (va) out[oa + k * oes] = xa;
+                    if (vb) out[obb + k * oes] = xb;
+                }
+            } else {
+                T *out = reinterpret_cast<T*>(P.out);
+                C const *rtw = reinterpret_cast<C const*>(P.rtw);
+                T s = P.do_scale ? sc : (T)1;
+                for (int k = t; k < N; k += TT){
+                    C zk = xch[xi(k)], zn = xch[xi((k == 0) ? 0 : N - k)];
+                    C w = __ldg(rtw + k);
+                    T ax = zk.x + zn.x, ay = zk.y - zn.y;
+                    T bx = zk.y + zn.y, by = -(zk.x - zn.x);
+                    int ko = sine ? (N - 1 - k) : k;
+                    if (va) out[oa + ko * oes] = (w.x * ax - w.y * ay) * s;
+                    if (vb) out[obb + ko * oes] = (w.x * bx - w.y * by) * s;
+                }
+            }
+        } else if constexpr (KIND == PK_C2R_BWD){
+            auto ld0 = [&](int p) -> C {
+                int pp = (2 * p <= N) ? p : N - p;
+                bool cj = (2 * p > N);
+                bool real_only = (pp == 0) || (2 * pp == N);
+                C xa, xb;
+                if (COLS){ xa = tb[pp * (2 * TPB) + 2 * loc]; xb = tb[pp * (2 * TPB) + 2 * loc + 1]; }
+                else { xa = tb[(2 * loc) * H + pp]; xb = tb[(2 * loc + 1) * H + pp]; }
+                if (real_only){ xa.y = 0; xb.y = 0; }
+                if (cj){ xa.y = -xa.y; xb.y = -xb.y; }
+                C z; z.x = xa.x - xb.y; z.y = xa.y + xb.x;
+                return z;
+            };
+            T *out = reinterpret_cast<T*>(P.out);
+            T s = P.do_scale ? sc : (T)1;
+            auto st = [&](int p, C x){
+                if (va) out[oa + p * oes] = x.x * s;
+                if (vb) out[obb + p * oes] = x.y * s;
+            };
+            pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+        } else {
+            // PK_R2R_BWD: V[k] = 2 exp(i pi k / 2N) (Y[k] - i Y[N-k]), two lines per FFT
+            C const *rtw = reinterpret_cast<C const*>(P.rtw);
+            auto yv = [&](int which, int k) -> T {
+                if (k >= N) return (T)0;
+                int kk = sine ? (N - 1 - k) : k;
+                if (COLS){ C z = tb[kk * TPB + loc]; return which ? z.y : z.x; }
+                return tr[(2 * loc + which) * N + kk];
+            };
+            auto ld0 = [&](int p) -> C {
+                C w = __ldg(rtw + p); w.y = -w.y;
+                T a0 = yv(0, p), a1 = (p == 0) ? (T)0 : yv(0, N - p);
+                T b0 = yv(1, p), b1 = (p == 0) ? (T)0 : yv(1, N - p);
+                C va_, vb_;
+                va_.x = 2 * (w.x * a0 + w.y * a1); va_.y = 2 * (w.y * a0 - w.x * a1);
+                vb_.x = 2 * (w.x * b0 + w.y * b1); vb_.y = 2 * (w.y * b0 - w.x * b1);
+                C z; z.x = va_.x - vb_.y; z.y = va_.y + vb_.x;
+                return z;
+            };
+            T *out = reinterpret_cast<T*>(P.out);
+            T s = P.do_scale ? sc : (T)1;
+            auto st = [&](int n, C x){
+                int m = (2 * n < N) ? 2 * n : 2 * (N - 1 - n) + 1;
+                T sg = (sine && (m & 1)) ? -s : s;
+                if (va) out[oa + m * oes] = x.x * sg;
+                if (vb) out[obb + m * oes] = x.y * sg;
+            };
+            pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+        }
         __syncthreads();
     }
 }

@@ -1,5 +1,9 @@
-// Host dispatch of the pipelined power-of-two kernels for one precision.
-// Included by gbfft_pipe_f32.cu (GB_T = float) and gbfft_pipe_f64.cu (GB_T = double).
+// Host dispatch of the pipelined power-of-two kernels for one precision and
+// one group of kinds.  Included by the gbfft_pipe_*.cu units with
+//   GB_T          float or double
+//   GB_PIPE_NAME  the exported dispatcher
+//   GB_GROUP      0: c2c (forward, backward), 1: r2c + c2r, 2: r2r forward + backward
+// so that the instantiations compile in parallel.
 #include "gbfft_internal.h"
 #include "gbfft_pipe.cuh"
 #include <atomic>
@@ -9,28 +13,44 @@ namespace gbfft {
 
 namespace {
 
-template<int N, bool FWD, bool COLS>
-bool run_pipe(cudaStream_t s, PipeArgs const &a){
+template<int N, int KIND, bool COLS, int LOADER>
+bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     using T = GB_T;
     using C = c_t<T>;
+    constexpr bool PAIRED = pipe_paired(KIND);
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
-    constexpr int SMEM = pipe_smem(N, sizeof(C), COLS);
-    constexpr int THREADS = TPB * pipe_tt(N);
-    auto kern = k_c2c_pipe<T, N, FWD, COLS>;
-    // applicability: whole tiles, contiguous tile rows / lines, 16-byte aligned copies
-    if (a.G % TPB != 0) return false;
-    if ((reinterpret_cast<uintptr_t>(a.in) & 15) != 0) return false;
-    if (COLS){
-        if (a.Li.dist != 1 || a.Li.count % TPB != 0) return false;
-        if (((long long)a.Li.estride * (long long)sizeof(C)) % 16 != 0) return false;
-        if (((long long)a.Li.bstride * (long long)sizeof(C)) % 16 != 0) return false;
-        if ((TPB * sizeof(C)) % 16 != 0) return false;
+    constexpr int SMEM = pipe_smem(N, sizeof(C), COLS, KIND);
+    constexpr int THREADS = pipe_threads(N, sizeof(C), COLS);
+    constexpr int IN_ES = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) ? (int)sizeof(T) : (int)sizeof(C);
+    constexpr int ROWS = (KIND == PK_C2R_BWD) ? N / 2 + 1 : N;
+    constexpr int WIDTH = PAIRED ? 2 * TPB : TPB;
+    constexpr int LINE_LEN = ROWS;
+    constexpr int UNITS = PAIRED ? 2 : 1;
+    Layout const &Li = a.Li;
+    uintptr_t base = reinterpret_cast<uintptr_t>(a.in);
+    if (a.G <= 0) return true;
+    if (a.G % Li.count != 0) return false;
+    long long blocks = a.G / Li.count;
+    PipeParams P{};
+    CUtensorMap tmap;
+    std::memset(&tmap, 0, sizeof(tmap));
+    if constexpr (LOADER == LD_TENSOR){
+        if (Li.dist != 1 || (base & 15) || ((WIDTH * IN_ES) % 16) != 0) return false;
+        int swap = 0;
+        if (!encode_column_tmap(&tmap, a.in, IN_ES, Li.count, ROWS, blocks, Li.estride, Li.bstride, WIDTH,
+                                ROWS < 256 ? ROWS : 256, &swap))
+            return false;
+        P.tswap = swap;
+    } else if constexpr (LOADER == LD_BULK){
+        if (Li.dist != LINE_LEN) return false;
+        if (blocks > 1 && Li.bstride != Li.count * LINE_LEN) return false;
+        if ((base & 15) || ((long long)a.G * LINE_LEN * IN_ES) % 16 != 0 ||
+            ((long long)TPB * UNITS * LINE_LEN * IN_ES) % 16 != 0)
+            return false;
     } else {
-        if (a.Li.dist != N) return false;
-        if (a.Li.count % TPB != 0 && a.Li.bstride != a.Li.count * N) return false;
-        if (((long long)a.Li.bstride * (long long)sizeof(C)) % 16 != 0) return false;
-        if ((N * sizeof(C)) % 16 != 0) return false;
+        if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }
+    auto kern = k_pipe<T, N, KIND, COLS, LOADER>;
     static std::atomic<unsigned long long> ready{0};
     static int blocks_per_sm[64] = {0};
     int dev = 0;
@@ -44,48 +64,65 @@ bool run_pipe(cudaStream_t s, PipeArgs const &a){
         blocks_per_sm[dev & 63] = std::max(nb, 1);
         ready.fetch_or(bit);
     }
-    long long ntiles = a.G / TPB;
-    long long grid = std::min<long long>(ntiles, (long long)num_sms() * blocks_per_sm[dev & 63]);
-    if (grid <= 0) return true;
-    CUtensorMap tmap;
-    std::memset(&tmap, 0, sizeof(tmap));
-    int tswap = 0;
+    P.Li = a.Li; P.Lo = a.Lo; P.in = a.in; P.out = a.out; P.tw = a.tw; P.rtw = a.rtw;
+    P.G = a.G; P.scale = a.scale; P.do_scale = (a.scale != 1.0); P.sine = a.sine; P.status = a.status;
     if (COLS){
-        long long blocks = a.G / a.Li.count;
-        if (!encode_column_tmap(&tmap, a.in, (int)sizeof(C), a.Li.count, N, blocks, a.Li.estride, a.Li.bstride,
-                                TPB, std::min(N, 256), &tswap))
-            return false;
+        P.tiles_per_block = (Li.count + WIDTH - 1) / WIDTH;
+        P.ntiles = blocks * P.tiles_per_block;
+    } else {
+        P.tiles_per_block = 0;
+        P.ntiles = (a.G + (long long)TPB * UNITS - 1) / ((long long)TPB * UNITS);
     }
-    kern<<<(unsigned)grid, THREADS, SMEM, s>>>(a.Li, a.Lo, (C const*)a.in, (C*)a.out, (C const*)a.tw, ntiles,
-                                              (T)a.scale, a.do_scale, a.status, tmap, tswap);
+    long long grid = std::min<long long>(P.ntiles, (long long)num_sms() * blocks_per_sm[dev & 63]);
+    kern<<<(unsigned)grid, THREADS, SMEM, s>>>(P, tmap);
     check_cuda(cudaPeekAtLastError(), "pipelined fft kernel launch");
     return true;
 }
 
-template<bool FWD, bool COLS>
-bool dispatch_n(cudaStream_t s, int N, PipeArgs const &a){
-    switch (N){
-        case 2: return run_pipe<2, FWD, COLS>(s, a);
-        case 4: return run_pipe<4, FWD, COLS>(s, a);
-        case 8: return run_pipe<8, FWD, COLS>(s, a);
-        case 16: return run_pipe<16, FWD, COLS>(s, a);
-        case 32: return run_pipe<32, FWD, COLS>(s, a);
-        case 64: return run_pipe<64, FWD, COLS>(s, a);
-        case 128: return run_pipe<128, FWD, COLS>(s, a);
-        case 256: return run_pipe<256, FWD, COLS>(s, a);
-        case 512: return run_pipe<512, FWD, COLS>(s, a);
-        case 1024: return run_pipe<1024, FWD, COLS>(s, a);
-        case 2048: return run_pipe<2048, FWD, COLS>(s, a);
-        case 4096: return run_pipe<4096, FWD, COLS>(s, a);
-        default: return false;
+template<int N, int KIND>
+bool run_kind(cudaStream_t s, bool cols, PipeLaunch const &a){
+    constexpr bool REAL_IN = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD);
+    if (!cols) return run_pipe<N, KIND, false, LD_BULK>(s, a);
+    if constexpr (KIND != PK_C2R_BWD){
+        if (run_pipe<N, KIND, true, LD_TENSOR>(s, a)) return true;
     }
+    if constexpr (!REAL_IN){
+        return run_pipe<N, KIND, true, LD_CPASYNC>(s, a);
+    }
+    return false;
+}
+
+template<int N>
+bool run_group(cudaStream_t s, int kind, bool cols, PipeLaunch const &a){
+#if GB_GROUP == 0
+    if (kind == PK_C2C_FWD) return run_kind<N, PK_C2C_FWD>(s, cols, a);
+    if (kind == PK_C2C_BWD) return run_kind<N, PK_C2C_BWD>(s, cols, a);
+#elif GB_GROUP == 1
+    if (kind == PK_R2C_FWD) return run_kind<N, PK_R2C_FWD>(s, cols, a);
+    if (kind == PK_C2R_BWD) return run_kind<N, PK_C2R_BWD>(s, cols, a);
+#else
+    if (kind == PK_R2R_FWD) return run_kind<N, PK_R2R_FWD>(s, cols, a);
+    if (kind == PK_R2R_BWD) return run_kind<N, PK_R2R_BWD>(s, cols, a);
+#endif
+    return false;
 }
 
 } // namespace
 
-bool GB_PIPE_NAME(cudaStream_t s, int N, bool fwd, bool cols, PipeArgs const &a){
-    if (cols) return fwd ? dispatch_n<true, true>(s, N, a) : dispatch_n<false, true>(s, N, a);
-    return fwd ? dispatch_n<true, false>(s, N, a) : dispatch_n<false, false>(s, N, a);
+bool GB_PIPE_NAME(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a){
+    constexpr bool DBL = sizeof(GB_T) == 8;
+    switch (N){
+        case 16: return run_group<16>(s, kind, cols, a);
+        case 32: return run_group<32>(s, kind, cols, a);
+        case 64: return run_group<64>(s, kind, cols, a);
+        case 128: return run_group<128>(s, kind, cols, a);
+        case 256: return run_group<256>(s, kind, cols, a);
+        case 512: return run_group<512>(s, kind, cols, a);
+        case 1024: return run_group<1024>(s, kind, cols, a);
+        case 2048: return run_group<2048>(s, kind, cols, a);
+        case 4096: if constexpr (!DBL) return run_group<4096>(s, kind, cols, a); else return false;
+        default: return false;
+    }
 }
 
 } // namespace gbfft

@@ -410,3 +410,42 @@ def test_power_of_two_kernel_variants(gb, variant, prec):
         assert gb.device_status() == 0
     finally:
         gb.set_kernel_variant(0)
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_power_of_two_real_kernel_variants(gb, variant, prec):
+    """r2c / c2r and DCT / DST through both kernel families: line tiles, column
+    tiles with TMA tensor maps and cp.async (odd half-spectrum widths, partial
+    tiles), every r2c direction, two orders."""
+    gb.set_kernel_variant(variant)
+    try:
+        rng = np.random.default_rng(40 + variant + 2 * prec)
+        for size in [(64, 32, 16), (32, 128, 16), (256, 16, 32), (16, 16, 512)]:
+            n = int(np.prod(size))
+            x = rng.standard_normal(n).astype(rdt(prec))
+            for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 0, 1), (2, 0, 1))]:
+                ib = gb.box3d((0, 0, 0), [s - 1 for s in size], io)
+                for rd in range(3):
+                    cb = ib.r2c(rd)
+                    p = gb.fft3d_r2c(ib, gb.box3d(cb.low, cb.high, oo), rd)
+                    xin = dev(x)
+                    y = torch.empty(p.size_outbox(), dtype=torch.complex64 if prec == 0 else torch.complex128,
+                                    device="cuda")
+                    p.forward(xin, y, gb.scale.full)
+                    assert O.rel_l2(host(y), O.fft3d_r2c(x, size, rd, io, oo, 1)) < TOL[prec], (size, rd, io)
+                    z = torch.empty_like(xin)
+                    p.backward(y, z)
+                    assert O.rel_l2(host(z), x) < 3 * TOL[prec], (size, rd, io, "c2r")
+                for rk, ok in ((gb.kind.cos, O.COS), (gb.kind.sin, O.SIN)):
+                    p = gb.rtransform(rk, ib, gb.box3d((0, 0, 0), [s - 1 for s in size], oo))
+                    xin = dev(x)
+                    y = torch.empty_like(xin)
+                    p.forward(xin, y)
+                    assert O.rel_l2(host(y), O.rtransform(ok, x, size, io, oo)) < TOL[prec], (size, rk, io)
+                    z = torch.empty_like(xin)
+                    p.backward(y, z, gb.scale.full)
+                    assert O.rel_l2(host(z), x) < 3 * TOL[prec], (size, rk, io, "bwd")
+        assert gb.device_status() == 0
+    finally:
+        gb.set_kernel_variant(0)
