@@ -310,6 +310,8 @@ WORKLOADS = {
     "z2z512": ("c2c", (512, 512, 512), 1),
     "c2c1024x1024x512": ("c2c", (1024, 1024, 512), 0),
     "z2z64": ("c2c", (64, 64, 64), 1),
+    # small case (256 MiB, above L2) for ncu captures of the c2c pass kernels
+    "c2c512x512x128": ("c2c", (512, 512, 128), 0),
 }
 
 

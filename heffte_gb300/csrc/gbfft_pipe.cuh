@@ -216,8 +216,14 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     // tile -> (block, first column) for column tiles, first line for line tiles
     auto tile_origin = [&](long long tile, long long &blk, long long &c0){
         if (COLS){
-            blk = tile / P.tiles_per_block;
-            c0 = (tile - blk * P.tiles_per_block) * WIDTH;
+            if (tile < 0x7fffffffLL && P.tiles_per_block < 0x7fffffffLL){
+                unsigned q = (unsigned)tile / (unsigned)P.tiles_per_block;
+                blk = q;
+                c0 = (long long)((unsigned)tile - q * (unsigned)P.tiles_per_block) * WIDTH;
+            } else {
+                blk = tile / P.tiles_per_block;
+                c0 = (tile - blk * P.tiles_per_block) * WIDTH;
+            }
         } else {
             blk = 0;
             c0 = tile * (long long)TPB * units_per;   // first line
@@ -256,7 +262,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
                 constexpr int RSTEP = NT / WIDTH;
                 int c = tid % WIDTH, r = tid / WIDTH;
                 bool valid = (c0 + c) < Li.count;
-                long long col = valid ? base_of_fast(Li, blk * Li.count + c0 + c) : 0;
+                long long col = valid ? blk * Li.bstride + (c0 + c) * Li.dist : 0;
                 unsigned char const *src = reinterpret_cast<unsigned char const*>(P.in) + col * IN_ES;
                 #pragma unroll 4
                 for (; r < ROWS; r += RSTEP){
@@ -268,7 +274,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
                 for (int e = tid; e < ROWS * WIDTH; e += NT){
                     int r = e / WIDTH, c = e - r * WIDTH;
                     bool valid = (c0 + c) < Li.count;
-                    long long off = valid ? base_of_fast(Li, blk * Li.count + c0 + c) * IN_ES + r * rstride : 0;
+                    long long off = valid ? (blk * Li.bstride + (c0 + c) * Li.dist) * IN_ES + r * rstride : 0;
                     unsigned char const *src = reinterpret_cast<unsigned char const*>(P.in) + off;
                     if constexpr (IN_ES == 16) cp_async_16(dst + (size_t)e * 16, src, valid);
                     else cp_async_8(dst + (size_t)e * 8, src, valid);
@@ -303,21 +309,22 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         long long blk, c0;
         tile_origin(tile, blk, c0);
         // transforms of this thread's unit
-        long long ga, gb;
         bool va, vb;
+        long long oa = 0, obb = 0;
         if (COLS){
+            // column ca of block blk: the output offset needs no division
             long long ca = c0 + (long long)loc * units_per;
             va = ca < Li.count;
             vb = PAIRED ? (ca + 1 < Li.count) : false;
-            ga = blk * Li.count + ca;
-            gb = ga + 1;
+            oa = blk * Lo.bstride + ca * Lo.dist;
+            obb = oa + Lo.dist;
         } else {
-            ga = c0 + (long long)loc * units_per;
-            gb = ga + 1;
+            long long ga = c0 + (long long)loc * units_per, gb = ga + 1;
             va = ga < P.G;
             vb = PAIRED ? (gb < P.G) : false;
+            if (va) oa = base_of_fast(Lo, ga);
+            if (vb) obb = base_of_fast(Lo, gb);
         }
-        long long oa = va ? base_of_fast(Lo, ga) : 0, obb = vb ? base_of_fast(Lo, gb) : 0;
         long long oes = Lo.estride;
         T const *tr = reinterpret_cast<T const*>(tb);
         int sine = P.sine;
