@@ -285,8 +285,11 @@ def ours(args, rank, world, local_rank):
                    "global_batch": world, "parallelism": f"replicas x{world}",
                    "l2": f"inputs {N * esize / 2**30:.2f} GiB > 129 MB L2 (no flush needed)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "kernel": "k_c2c " + ("column" if dom else "line") + f" pass along dim {dom}",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     # DRAM read+write bytes per launch of the column pass kernel, from the ncu
+                     # launch list of this command (profiles/k_pipe_c2c_512cube_fp32.md)
+                     "traffic": 2.083e9 if (n == 512 and prec == 0) else None,
+                     "kernel": "k_pipe " + ("column" if dom else "line") + f" pass along dim {dom}",
                      "algorithmic_bytes_per_launch": pass_bytes,
                      "per_pass_ms": {str(d): per_launch[d] for d in per_launch},
                      "step_bytes": step_bytes, "step_gbs": step_bytes / (ms_step / 1e3) / 1e9,
