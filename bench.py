@@ -315,7 +315,56 @@ WORKLOADS = {
     "z2z64": ("c2c", (64, 64, 64), 1),
     # small case (256 MiB, above L2) for ncu captures of the c2c pass kernels
     "c2c512x512x128": ("c2c", (512, 512, 128), 0),
+    # 256 r2c float boxes, sides i.i.d. from {16, 24, ..., 128} (seed 256), one persistent launch
+    "batch256": ("batch", None, 0),
+    # the same after autotuning the radix plan / tile size of every side length
+    "batch256tuned": ("batch", "tuned", 0),
 }
+
+BATCH_SIDES = [16, 24, 32, 40, 48, 64, 80, 96, 128]
+
+
+def batch_sizes(nboxes=256, seed=256):
+    rng = np.random.default_rng(seed)
+    return [tuple(int(v) for v in rng.choice(BATCH_SIDES, 3)) for _ in range(nboxes)]
+
+
+def run_batch_workload(name, steps, warmup, tune_cache=None):
+    import torch
+    import heffte_gb300 as gb
+    sizes = batch_sizes()
+    stream = torch.cuda.current_stream()
+    if tune_cache is not None:
+        gb.tune(0, BATCH_SIDES, tune_cache, stream=stream)
+    b = gb.boxbatch(gb.kind.r2c, sizes, 0, stream=stream)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    x = torch.randn(b.input_size(), device="cuda", generator=gen)
+    y = torch.empty(b.output_size(), dtype=torch.complex64, device="cuda")
+    z = torch.empty_like(x)
+    w = torch.empty(b.workspace_size(), dtype=torch.complex64, device="cuda")
+
+    def step():
+        b.forward(x, y, gb.scale.full)
+        b.backward(y, z, w, gb.scale.none)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    err = float((z - x).abs().max().item())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    flops = sum(2 * flops_per_transform(s[0] * s[1] * s[2]) for s in sizes)
+    byts = sum(2 * algorithmic_bytes("r2c", s, 0) for s in sizes)
+    peak, _ = peaks()
+    return {"workload": name, "boxes": len(sizes), "ms_per_step": ms, "gflops": flops / (ms / 1e3) / 1e9,
+            "gbs": byts / (ms / 1e3) / 1e9, "hbm_frac": byts / (ms / 1e3) / 1e9 / peak,
+            "roundtrip_max_abs": err, "launches_per_step": 2, "tuned": tune_cache is not None}
 
 
 def algorithmic_bytes(kind, size, prec):
@@ -334,6 +383,12 @@ def run_workload(name, steps, warmup):
     import torch
     import heffte_gb300 as gb
     kind, size, prec = WORKLOADS[name]
+    if kind == "batch":
+        cache = None
+        if size == "tuned":
+            import tempfile
+            cache = os.path.join(tempfile.mkdtemp(), "tune.tsv")
+        return run_batch_workload(name, steps, warmup, cache)
     N = size[0] * size[1] * size[2]
     stream = torch.cuda.current_stream()
     box = gb.box3d((0, 0, 0), [s - 1 for s in size])

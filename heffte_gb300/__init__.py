@@ -78,6 +78,20 @@ def lib():
     L.heffte_gb300_backward.argtypes = [vp, i, vp, vp, vp, i]
     L.heffte_gb300_forward_batch.argtypes = [vp, i, i, vp, vp, vp, i]
     L.heffte_gb300_backward_batch.argtypes = [vp, i, i, vp, vp, vp, i]
+    L.heffte_gb300_boxbatch_create.argtypes = [i, i, i, ctypes.POINTER(ctypes.c_int), vp, ctypes.POINTER(vp)]
+    L.heffte_gb300_boxbatch_destroy.argtypes = [vp]
+    for f in ("input_offset", "output_offset"):
+        getattr(L, "heffte_gb300_boxbatch_" + f).argtypes = [vp, i]
+        getattr(L, "heffte_gb300_boxbatch_" + f).restype = ll
+    for f in ("input_size", "output_size", "workspace_size"):
+        getattr(L, "heffte_gb300_boxbatch_" + f).argtypes = [vp]
+        getattr(L, "heffte_gb300_boxbatch_" + f).restype = ll
+    L.heffte_gb300_boxbatch_forward.argtypes = [vp, vp, vp, i]
+    L.heffte_gb300_boxbatch_backward.argtypes = [vp, vp, vp, vp, i]
+    L.heffte_gb300_tune.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_int)]
+    L.heffte_gb300_tune_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+    L.heffte_gb300_tuned_choice.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -348,3 +362,68 @@ def device_status(reset=False):
     v = ctypes.c_int(-1)
     check(lib().heffte_gb300_device_status(ctypes.byref(v), int(reset)))
     return v.value
+
+
+class boxbatch:
+    """Many small 3-D boxes of uneven sizes transformed in one persistent,
+    graph-replayed launch (kind.r2c or kind.c2c; r2c along dimension 0)."""
+
+    def __init__(self, bkind, sizes, prec=0, stream=None):
+        flat = [int(v) for s in sizes for v in s]
+        self.sizes = [tuple(s) for s in sizes]
+        self.prec = prec
+        self._h = ctypes.c_void_p()
+        check(lib().heffte_gb300_boxbatch_create(bkind, prec, len(self.sizes), (ctypes.c_int * len(flat))(*flat),
+                                                 _stream_handle(stream), ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.heffte_gb300_boxbatch_destroy(h)
+
+    def input_offset(self, box):
+        return lib().heffte_gb300_boxbatch_input_offset(self._h, box)
+
+    def output_offset(self, box):
+        return lib().heffte_gb300_boxbatch_output_offset(self._h, box)
+
+    def input_size(self):
+        return lib().heffte_gb300_boxbatch_input_size(self._h)
+
+    def output_size(self):
+        return lib().heffte_gb300_boxbatch_output_size(self._h)
+
+    def workspace_size(self):
+        return lib().heffte_gb300_boxbatch_workspace_size(self._h)
+
+    def forward(self, inarray, outarray, scaling=scale.none):
+        check(lib().heffte_gb300_boxbatch_forward(self._h, _ptr(inarray), _ptr(outarray), scaling))
+
+    def backward(self, inarray, outarray, workspace, scaling=scale.none):
+        check(lib().heffte_gb300_boxbatch_backward(self._h, _ptr(inarray), _ptr(outarray), _ptr(workspace), scaling))
+
+
+def tune(prec, lengths, cache_path=None, stream=None):
+    """Autotunes the radix plan / tile size of each length; returns how many were measured."""
+    arr = (ctypes.c_int * len(lengths))(*[int(n) for n in lengths])
+    m = ctypes.c_int(0)
+    check(lib().heffte_gb300_tune(prec, len(lengths), arr, cache_path.encode() if cache_path else None,
+                                  _stream_handle(stream), ctypes.byref(m)))
+    return m.value
+
+
+def tune_load(cache_path):
+    n = ctypes.c_int(0)
+    check(lib().heffte_gb300_tune_load(cache_path.encode(), ctypes.byref(n)))
+    return n.value
+
+
+def tune_clear():
+    check(lib().heffte_gb300_tune_clear())
+
+
+def tuned_choice(prec, length):
+    rad = (ctypes.c_int * 16)()
+    nr, tpb, us = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+    check(lib().heffte_gb300_tuned_choice(prec, length, rad, ctypes.byref(nr), ctypes.byref(tpb), ctypes.byref(us)))
+    return list(rad[:nr.value]), tpb.value, us.value

@@ -1,0 +1,365 @@
+// Batches of many small 3-D r2c / c2r transforms of uneven sizes in ONE
+// persistent kernel launch, replayed as a CUDA graph.
+//
+// The work of a batch is a list of "units": one 1-D pass of one box (r2c along
+// x, then c2c along y and z; the reverse order backward).  Units are cut into
+// tiles and enumerated pass-major; persistent CTAs take tiles from a global
+// atomic counter.  A tile of pass p of box b first waits until every tile of
+// pass p-1 of box b has completed (a per-unit completion counter).  Because
+// tiles are handed out in order, the tiles waited for have already been taken
+// by running CTAs, so the wait always ends; it is bounded anyway, and a wait
+// that gives up records DEV_TIMEOUT_DEPENDENCY in the device status word.
+// Data written by other CTAs is read with L1-bypassing loads (tile_* device
+// functions use __ldcg).  Radix plans and tile sizes per transform length come
+// from the autotuner when it has measured them (gbfft_tune.cu).
+#include "gbfft_batch.h"
+#include "gbfft_kernels.cuh"
+#include "gbfft_ptx.cuh"
+#include <numeric>
+
+namespace gbfft {
+
+struct BatchUnit {
+    int kind;            // K_R2C, K_C2R, K_C2C_F, K_C2C_B
+    int cols;            // column layout (1) or lines (0)
+    int plan;            // index into the plan table
+    int tpb;             // transforms (or pairs) per tile
+    int src, dst;        // buffers: 0 input, 1 output, 2 workspace
+    int dep;             // unit that must complete first (-1: none)
+    int last;            // carries the scale
+    long long G;         // transforms of this pass
+    long long tiles, tile0;
+    long long in_off, out_off;   // element offsets into the source / destination buffer
+    Layout Li, Lo;
+    double scale;
+};
+
+enum { DEV_TIMEOUT_DEPENDENCY = 2 };
+
+// scaling: 0 none, 1 full (1/N of each box), 2 symmetric
+template<typename T>
+__global__ void __launch_bounds__(256)
+k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
+        c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
+        long long total_tiles, int *status, int scaling){
+    using C = c_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C*>(smraw);
+    __shared__ long long s_tile;
+    __shared__ int s_unit;
+    int tid = threadIdx.x;
+    while (true){
+        if (tid == 0){
+            s_tile = (long long)atomicAdd(work_counter, 1ull);
+            int lo = 0, hi = nunits - 1;
+            if (s_tile < total_tiles){
+                while (lo < hi){          // last unit with tile0 <= s_tile
+                    int mid = (lo + hi + 1) >> 1;
+                    if (units[mid].tile0 <= s_tile) lo = mid; else hi = mid - 1;
+                }
+            }
+            s_unit = lo;
+        }
+        __syncthreads();
+        long long gt = s_tile;
+        int u = s_unit;
+        if (gt >= total_tiles) return;
+        BatchUnit const &U = units[u];
+        bool ok = true;
+        if (tid == 0 && U.dep >= 0){
+            long long need = units[U.dep].tiles;
+            volatile int *d = done + U.dep;
+            if (*d < need){
+                long long t0 = clock64();
+                while (*d < need){
+                    if (clock64() - t0 > 4000000000LL){ atomicExch(status, DEV_TIMEOUT_DEPENDENCY); ok = false; break; }
+                }
+            }
+            __threadfence();
+        }
+        if (__syncthreads_or(!ok)) return;
+        long long lt = gt - U.tile0;
+        Plan1D const &P = plans[U.plan];
+        C const *tw = tws[U.plan];
+        unsigned char const *srcb = reinterpret_cast<unsigned char const*>(U.src == 0 ? bufs.in : (U.src == 1 ? bufs.out : bufs.work));
+        unsigned char *dstb = reinterpret_cast<unsigned char*>(U.dst == 1 ? bufs.out : bufs.work);
+        double f = (scaling == 0) ? 1.0 : ((scaling == 1) ? U.scale : sqrt(U.scale));
+        T sc = (T)f;
+        int dsc = U.last && scaling != 0;
+        switch (U.kind){
+            case K_R2C: {
+                T const *in = reinterpret_cast<T const*>(srcb) + U.in_off;
+                C *out = reinterpret_cast<C*>(dstb) + U.out_off;
+                if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                break;
+            }
+            case K_C2R: {
+                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
+                T *out = reinterpret_cast<T*>(dstb) + U.out_off;
+                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                break;
+            }
+            case K_C2C_F: {
+                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
+                C *out = reinterpret_cast<C*>(dstb) + U.out_off;
+                if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                break;
+            }
+            default: {
+                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
+                C *out = reinterpret_cast<C*>(dstb) + U.out_off;
+                if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                break;
+            }
+        }
+        // publish completion of this tile
+        __syncthreads();
+        if (tid == 0){
+            __threadfence();
+            atomicAdd(done + u, 1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static constexpr int kBatchThreads = 256;
+
+Batch::~Batch(){
+    if (fwd_exec) cudaGraphExecDestroy(fwd_exec);
+    if (bwd_exec) cudaGraphExecDestroy(bwd_exec);
+    if (fwd_graph) cudaGraphDestroy(fwd_graph);
+    if (bwd_graph) cudaGraphDestroy(bwd_graph);
+    for (void *p : device_allocs) cudaFree(p);
+}
+
+static int tile_tpb(Fft1D const &f, bool cols, bool paired, size_t csize, size_t smem_cap, int tune_tpb){
+    int T = f.plan.T;
+    int tpb = (tune_tpb > 0) ? tune_tpb : std::max(1, kBatchThreads / T);
+    tpb = std::min(tpb, std::max(1, kBatchThreads / T));
+    size_t unit = cols ? (size_t)f.N * csize : (size_t)(f.N + (f.N >> 4) + 1) * csize;
+    while (tpb > 1 && tpb * unit > smem_cap) tpb--;
+    (void)paired;
+    return tpb;
+}
+
+std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream){
+    if (kind != PK_R2C && kind != PK_C2C) throw Error(ST_UNSUPPORTED, "batches support c2c and r2c boxes");
+    if (prec != 0 && prec != 1) throw Error(ST_INVALID, "precision must be 0 or 1");
+    if (sizes.empty()) throw Error(ST_INVALID, "empty batch");
+    auto b = std::make_unique<Batch>();
+    b->kind = kind; b->prec = prec; b->sizes = sizes; b->stream = stream;
+    size_t csize = (prec == 0) ? sizeof(float2) : sizeof(double2);
+    size_t rsize = csize / 2;
+    bool r2c = (kind == PK_R2C);
+    long long in_off = 0, out_off = 0;
+    for (auto const &s : sizes){
+        for (int d = 0; d < 3; d++){
+            if (s[d] < 1 || !supported_length(s[d], prec))
+                throw Error(ST_UNSUPPORTED, "box side " + std::to_string(s[d]) + " is not supported");
+        }
+        long long n = (long long)s[0] * s[1] * s[2];
+        long long nc = r2c ? (long long)(s[0] / 2 + 1) * s[1] * s[2] : n;
+        b->in_offsets.push_back(in_off);
+        b->out_offsets.push_back(out_off);
+        in_off += n;
+        out_off += nc;
+    }
+    b->in_total = in_off;
+    b->out_total = out_off;
+    // distinct lengths -> plan table (tuned radix plans where available)
+    std::vector<int> lens;
+    for (auto const &s : sizes) for (int d = 0; d < 3; d++) lens.push_back(s[d]);
+    std::sort(lens.begin(), lens.end());
+    lens.erase(std::unique(lens.begin(), lens.end()), lens.end());
+    std::map<int, int> plan_of;
+    std::vector<Plan1D> plans;
+    std::vector<void const*> tws;
+    std::vector<int> tpb_hint;
+    for (int N : lens){
+        TuneChoice tc = tuned_choice(N, prec);
+        auto f = get_fft1d(N, tc.radices);
+        plan_of[N] = (int)plans.size();
+        plans.push_back(f->plan);
+        tws.push_back(f->twiddles(prec, stream));
+        b->ffts.push_back(f);
+        tpb_hint.push_back(tc.tpb);
+    }
+    size_t smem_cap = 48 * 1024;
+    // units: forward = (r2c|c2c x), c2c y, c2c z; backward = c2c z, c2c y, (c2r|c2c x)
+    auto build = [&](bool fwd, std::vector<BatchUnit> &units, long long &total){
+        std::vector<std::vector<BatchUnit>> per_pass(3);
+        for (size_t i = 0; i < sizes.size(); i++){
+            auto const &s = sizes[i];
+            Box3 rbox({0, 0, 0}, {s[0] - 1, s[1] - 1, s[2] - 1}, {0, 1, 2});
+            Box3 cbox = r2c ? rbox.r2c(0) : rbox;
+            double sc = 1.0 / (double)rbox.count();
+            int order_dims[3] = {0, 1, 2};
+            for (int k = 0; k < 3; k++){
+                int d = fwd ? order_dims[k] : order_dims[2 - k];
+                BatchUnit U{};
+                bool first = (k == 0), lastp = (k == 2);
+                bool is_r2x = r2c && d == 0;
+                U.kind = is_r2x ? (fwd ? K_R2C : K_C2R) : (fwd ? K_C2C_F : K_C2C_B);
+                Box3 const &sb = (is_r2x && fwd) ? rbox : cbox;
+                Box3 const &db = (is_r2x && !fwd) ? rbox : cbox;
+                U.Li = pass_layout(sb, d, {0, 1, 2});
+                U.Lo = pass_layout(db, d, {0, 1, 2});
+                U.cols = (d != 0);
+                U.G = rbox.count() / rbox.size[d];
+                U.plan = plan_of[(int)rbox.size[d]];
+                Fft1D const &f = *b->ffts[U.plan];
+                bool paired = is_r2x;
+                U.tpb = tile_tpb(f, U.cols, paired, csize, smem_cap, tpb_hint[U.plan]);
+                long long units_n = paired ? (U.G + 1) / 2 : U.G;
+                U.tiles = (units_n + U.tpb - 1) / U.tpb;
+                // buffers: forward input -> output (in place after the first pass);
+                // backward input -> workspace -> output (the input is preserved)
+                if (fwd){
+                    U.src = first ? 0 : 1;
+                    U.dst = 1;
+                    U.in_off = first ? b->in_offsets[i] : b->out_offsets[i];
+                    U.out_off = b->out_offsets[i];
+                } else {
+                    U.src = first ? 0 : 2;
+                    U.dst = lastp ? 1 : 2;
+                    U.in_off = b->out_offsets[i];
+                    U.out_off = lastp ? b->in_offsets[i] : b->out_offsets[i];
+                }
+                U.last = lastp ? 1 : 0;
+                U.scale = sc;
+                per_pass[k].push_back(U);
+            }
+        }
+        units.clear();
+        total = 0;
+        int nb = (int)sizes.size();
+        std::vector<int> pos(3 * nb);      // pos[k * nb + box] = unit index of pass k of box
+        for (int k = 0; k < 3; k++){
+            // larger boxes first within a pass (balances the tail)
+            std::vector<int> idx(nb);
+            std::iota(idx.begin(), idx.end(), 0);
+            std::stable_sort(idx.begin(), idx.end(), [&](int a, int c){ return per_pass[k][a].tiles > per_pass[k][c].tiles; });
+            for (int i : idx){
+                BatchUnit U = per_pass[k][i];
+                U.dep = (k == 0) ? -1 : pos[(k - 1) * nb + i];
+                U.tile0 = total;
+                total += U.tiles;
+                pos[k * nb + i] = (int)units.size();
+                units.push_back(U);
+            }
+        }
+    };
+    std::vector<BatchUnit> fu, bu;
+    build(true, fu, b->fwd_tiles);
+    build(false, bu, b->bwd_tiles);
+    b->nunits = (int)fu.size();
+    // device tables
+    auto dalloc = [&](size_t bytes) -> void* {
+        void *p = nullptr;
+        check_cuda(cudaMalloc(&p, std::max<size_t>(bytes, 16)), "cudaMalloc(batch tables)");
+        b->device_allocs.push_back(p);
+        return p;
+    };
+    b->d_fwd_units = dalloc(fu.size() * sizeof(BatchUnit));
+    b->d_bwd_units = dalloc(bu.size() * sizeof(BatchUnit));
+    b->d_plans = dalloc(plans.size() * sizeof(Plan1D));
+    b->d_tws = dalloc(tws.size() * sizeof(void*));
+    b->d_counters = dalloc(sizeof(unsigned long long) + fu.size() * sizeof(int));
+    check_cuda(cudaMemcpy(b->d_fwd_units, fu.data(), fu.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice), "copy units");
+    check_cuda(cudaMemcpy(b->d_bwd_units, bu.data(), bu.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice), "copy units");
+    check_cuda(cudaMemcpy(b->d_plans, plans.data(), plans.size() * sizeof(Plan1D), cudaMemcpyHostToDevice), "copy plans");
+    check_cuda(cudaMemcpy(b->d_tws, tws.data(), tws.size() * sizeof(void*), cudaMemcpyHostToDevice), "copy twiddle table");
+    // launch geometry: persistent CTAs, as many as fit
+    size_t smem = 0;
+    for (auto const *v : {&fu, &bu})
+        for (auto const &U : *v){
+            Fft1D const &f = *b->ffts[U.plan];
+            size_t unit = U.cols ? (size_t)f.N * csize : (size_t)(f.N + (f.N >> 4) + 1) * csize;
+            smem = std::max(smem, unit * U.tpb);
+        }
+    b->smem = smem;
+    int nb_sm = 1;
+    if (prec == 0){
+        check_cuda(cudaFuncSetAttribute(k_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, k_batch<float>, kBatchThreads, smem), "occupancy");
+    } else {
+        check_cuda(cudaFuncSetAttribute(k_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, k_batch<double>, kBatchThreads, smem), "occupancy");
+    }
+    b->grid = std::max(1, nb_sm) * num_sms();
+    (void)rsize;
+    return b;
+}
+
+// Builds (once) the graph of one direction: reset the counters, run the kernel.
+static void build_graph(Batch &b, bool fwd){
+    cudaGraph_t &g = fwd ? b.fwd_graph : b.bwd_graph;
+    cudaGraphExec_t &e = fwd ? b.fwd_exec : b.bwd_exec;
+    check_cuda(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+    cudaMemsetParams ms{};
+    ms.dst = b.d_counters;
+    ms.value = 0;
+    ms.elementSize = 1;
+    ms.width = sizeof(unsigned long long) + (size_t)b.nunits * sizeof(int);
+    ms.height = 1;
+    cudaGraphNode_t mnode, knode;
+    check_cuda(cudaGraphAddMemsetNode(&mnode, g, nullptr, 0, &ms), "cudaGraphAddMemsetNode");
+    b.args_units = fwd ? b.d_fwd_units : b.d_bwd_units;
+    b.args_nunits = b.nunits;
+    b.args_plans = b.d_plans;
+    b.args_tws = b.d_tws;
+    b.args_bufs = BatchBufs{nullptr, nullptr, nullptr};
+    b.args_counter = reinterpret_cast<unsigned long long*>(b.d_counters);
+    b.args_done = reinterpret_cast<int*>(reinterpret_cast<char*>(b.d_counters) + sizeof(unsigned long long));
+    b.args_total = fwd ? b.fwd_tiles : b.bwd_tiles;
+    b.args_status = device_status();
+    b.args_scaling = 0;
+    void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
+                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling};
+    cudaKernelNodeParams kp{};
+    kp.func = (b.prec == 0) ? reinterpret_cast<void*>(k_batch<float>) : reinterpret_cast<void*>(k_batch<double>);
+    kp.gridDim = dim3((unsigned)b.grid);
+    kp.blockDim = dim3(kBatchThreads);
+    kp.sharedMemBytes = (unsigned)b.smem;
+    kp.kernelParams = args;
+    check_cuda(cudaGraphAddKernelNode(&knode, g, &mnode, 1, &kp), "cudaGraphAddKernelNode");
+    check_cuda(cudaGraphInstantiate(&e, g, 0), "cudaGraphInstantiate");
+    (fwd ? b.fwd_knode : b.bwd_knode) = knode;
+}
+
+void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
+    if (!in || !out) throw Error(ST_INVALID, "null pointer");
+    if (scaling < 0 || scaling > 2) throw Error(ST_INVALID, "invalid scaling");
+    if (!fwd && !work) throw Error(ST_INVALID, "the backward batch needs a workspace of size_workspace() elements");
+    cudaGraphExec_t &e = fwd ? fwd_exec : bwd_exec;
+    if (!e) build_graph(*this, fwd);
+    // point the kernel node at this call's buffers
+    args_units = fwd ? d_fwd_units : d_bwd_units;
+    args_nunits = nunits;
+    args_plans = d_plans;
+    args_tws = d_tws;
+    args_bufs = BatchBufs{in, out, work};
+    args_counter = reinterpret_cast<unsigned long long*>(d_counters);
+    args_done = reinterpret_cast<int*>(reinterpret_cast<char*>(d_counters) + sizeof(unsigned long long));
+    args_total = fwd ? fwd_tiles : bwd_tiles;
+    args_status = device_status();
+    args_scaling = scaling;
+    void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
+                    &args_total, &args_status, &args_scaling};
+    cudaKernelNodeParams kp{};
+    kp.func = (prec == 0) ? reinterpret_cast<void*>(k_batch<float>) : reinterpret_cast<void*>(k_batch<double>);
+    kp.gridDim = dim3((unsigned)grid);
+    kp.blockDim = dim3(kBatchThreads);
+    kp.sharedMemBytes = (unsigned)smem;
+    kp.kernelParams = args;
+    check_cuda(cudaGraphExecKernelNodeSetParams(e, fwd ? fwd_knode : bwd_knode, &kp), "cudaGraphExecKernelNodeSetParams");
+    check_cuda(cudaGraphLaunch(e, stream), "cudaGraphLaunch");
+}
+
+} // namespace gbfft

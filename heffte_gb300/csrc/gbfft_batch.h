@@ -1,0 +1,71 @@
+// Batched multi-box transforms and the per-length autotuner.
+#pragma once
+#include "gbfft_plan.h"
+#include <map>
+#include <string>
+
+namespace gbfft {
+
+// ---------------------------------------------------------------------------
+// autotuner (gbfft_tune.cu)
+// ---------------------------------------------------------------------------
+struct TuneChoice {
+    std::vector<int> radices;   // empty: default plan
+    int tpb = 0;                // transforms per tile of the generic kernels, 0: default
+    double us = 0;              // measured time of the choice (lines + columns probe)
+};
+
+// Choice for a length, from the tuning table (empty when never measured).
+TuneChoice tuned_choice(int N, int prec);
+// Candidate radix plans of a length (the default plan first).
+std::vector<std::vector<int>> radix_candidates(int N);
+// Measures every candidate of every length on the current device and keeps
+// the fastest; results are appended to `cache_path` (if not empty) after each
+// length, so an interrupted run resumes where it stopped.  Returns the number
+// of lengths measured (lengths already in the table are skipped).
+int tune_lengths(std::vector<int> const &lengths, int prec, cudaStream_t s, std::string const &cache_path);
+// Loads a cache written by tune_lengths for this device; returns entries read.
+int tune_load(std::string const &cache_path);
+void tune_clear();
+std::string device_key();
+
+// ---------------------------------------------------------------------------
+// batch of boxes (gbfft_batch.cu)
+// ---------------------------------------------------------------------------
+struct BatchBufs { void const *in; void *out; void *work; };
+
+struct Batch {
+    int kind = PK_R2C;
+    int prec = 0;
+    std::vector<std::array<int, 3>> sizes;
+    cudaStream_t stream = nullptr;
+    std::vector<long long> in_offsets, out_offsets;
+    long long in_total = 0, out_total = 0;
+    std::vector<std::shared_ptr<Fft1D>> ffts;
+    std::vector<void*> device_allocs;
+    void *d_fwd_units = nullptr, *d_bwd_units = nullptr, *d_plans = nullptr, *d_tws = nullptr, *d_counters = nullptr;
+    int nunits = 0;
+    long long fwd_tiles = 0, bwd_tiles = 0;
+    size_t smem = 0;
+    int grid = 0;
+    cudaGraph_t fwd_graph = nullptr, bwd_graph = nullptr;
+    cudaGraphExec_t fwd_exec = nullptr, bwd_exec = nullptr;
+    cudaGraphNode_t fwd_knode = nullptr, bwd_knode = nullptr;
+    // kernel-node arguments (the graph node points at these)
+    void *args_units = nullptr;
+    int args_nunits = 0;
+    void *args_plans = nullptr, *args_tws = nullptr;
+    BatchBufs args_bufs{};
+    unsigned long long *args_counter = nullptr;
+    int *args_done = nullptr;
+    long long args_total = 0;
+    int *args_status = nullptr;
+    int args_scaling = 0;
+    ~Batch();
+    long long workspace_elems() const { return out_total; }
+    void run(bool fwd, void const *in, void *out, void *work, int scaling);
+};
+
+std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream);
+
+} // namespace gbfft

@@ -1,5 +1,6 @@
 // extern "C" boundary of libheffte_gb300 (declarations in include/heffte_gb300.h).
 #include "gbfft_plan.h"
+#include "gbfft_batch.h"
 #include "../../include/heffte_gb300.h"
 #include <cstring>
 #include <new>
@@ -272,6 +273,85 @@ int heffte_gb300_forward_batch(heffte_gb300_plan plan, int batch, int prec, cons
 int heffte_gb300_backward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
                                 void *workspace, int scale){
     return exec(plan, false, batch, prec, input, output, workspace, scale);
+}
+
+// ---------------------------------------------------------------------------
+// batches of uneven boxes, autotuner
+// ---------------------------------------------------------------------------
+struct heffte_gb300_boxbatch_s { std::unique_ptr<Batch> b; };
+
+int heffte_gb300_boxbatch_create(int kind, int prec, int nboxes, const int *sizes, void *stream,
+                                 heffte_gb300_boxbatch *out){
+    return guard([&]{
+        if (!out || !sizes) throw Error(ST_INVALID, "null pointer");
+        *out = nullptr;
+        if (nboxes < 1) throw Error(ST_INVALID, "a batch needs at least one box");
+        std::vector<std::array<int, 3>> sz(nboxes);
+        for (int i = 0; i < nboxes; i++) sz[i] = {sizes[3 * i], sizes[3 * i + 1], sizes[3 * i + 2]};
+        auto b = make_batch(kind, prec, sz, as_stream(stream));
+        auto *h = new heffte_gb300_boxbatch_s;
+        h->b = std::move(b);
+        *out = h;
+    });
+}
+
+int heffte_gb300_boxbatch_destroy(heffte_gb300_boxbatch b){ return guard([&]{ delete b; }); }
+
+long long heffte_gb300_boxbatch_input_offset(heffte_gb300_boxbatch b, int box){
+    return (b && box >= 0 && box < (int)b->b->in_offsets.size()) ? b->b->in_offsets[box] : -1;
+}
+long long heffte_gb300_boxbatch_output_offset(heffte_gb300_boxbatch b, int box){
+    return (b && box >= 0 && box < (int)b->b->out_offsets.size()) ? b->b->out_offsets[box] : -1;
+}
+long long heffte_gb300_boxbatch_input_size(heffte_gb300_boxbatch b){ return b ? b->b->in_total : -1; }
+long long heffte_gb300_boxbatch_output_size(heffte_gb300_boxbatch b){ return b ? b->b->out_total : -1; }
+long long heffte_gb300_boxbatch_workspace_size(heffte_gb300_boxbatch b){ return b ? b->b->workspace_elems() : -1; }
+
+int heffte_gb300_boxbatch_forward(heffte_gb300_boxbatch b, const void *input, void *output, int scale){
+    return guard([&]{
+        if (!b) throw Error(ST_INVALID, "null batch");
+        b->b->run(true, input, output, nullptr, scale);
+        check_cuda(cudaPeekAtLastError(), "batched forward transform");
+    });
+}
+
+int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch b, const void *input, void *output, void *workspace, int scale){
+    return guard([&]{
+        if (!b) throw Error(ST_INVALID, "null batch");
+        b->b->run(false, input, output, workspace, scale);
+        check_cuda(cudaPeekAtLastError(), "batched backward transform");
+    });
+}
+
+int heffte_gb300_tune(int prec, int nlengths, const int *lengths, const char *cache_path, void *stream, int *measured){
+    return guard([&]{
+        if (!lengths && nlengths > 0) throw Error(ST_INVALID, "null pointer");
+        check_prec(prec);
+        std::vector<int> l(lengths, lengths + nlengths);
+        int m = tune_lengths(l, prec, as_stream(stream), cache_path ? std::string(cache_path) : std::string());
+        if (measured) *measured = m;
+    });
+}
+
+int heffte_gb300_tune_load(const char *cache_path, int *entries){
+    return guard([&]{
+        if (!cache_path) throw Error(ST_INVALID, "null path");
+        int n = tune_load(cache_path);
+        if (entries) *entries = n;
+    });
+}
+
+int heffte_gb300_tune_clear(void){ return guard([&]{ tune_clear(); }); }
+
+int heffte_gb300_tuned_choice(int prec, int length, int *radices, int *nradices, int *tpb, double *us){
+    return guard([&]{
+        if (!radices || !nradices || !tpb) throw Error(ST_INVALID, "null pointer");
+        TuneChoice c = tuned_choice(length, prec);
+        *nradices = (int)c.radices.size();
+        for (size_t i = 0; i < c.radices.size() && i < 16; i++) radices[i] = c.radices[i];
+        *tpb = c.tpb;
+        if (us) *us = c.us;
+    });
 }
 
 } // extern "C"

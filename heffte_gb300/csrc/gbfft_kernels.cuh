@@ -124,22 +124,34 @@ __device__ __forceinline__ int padded_len(int N){ return N + (N >> 4) + 1; }
 // ---------------------------------------------------------------------------
 // complex-to-complex
 // ---------------------------------------------------------------------------
+// Each kernel body is a per-tile device function (tile = block of TPB
+// transforms) so that the batched multi-box kernel can reuse it; threads
+// beyond TPB * T of a larger CTA stay inactive but join every barrier.
+template<typename T, int EMAX, bool FWD, bool COLS>
+__device__ __forceinline__ void tile_c2c(Plan1D const &P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out,
+                                         c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
+                                         long long tile, c_t<T> *sm){
+    using C = c_t<T>;
+    int loc, t;
+    thread_map<COLS>(TPB, P.T, loc, t);
+    long long g = tile * TPB + loc;
+    bool active = (g < G) && (t < P.T) && (loc < TPB);
+    long long ib = active ? base_of(Li, g) : 0, ob = active ? base_of(Lo, g) : 0;
+    long long ies = Li.estride, oes = Lo.estride;
+    // L2-only loads: in the batched kernel the data was written by other CTAs
+    // of the same launch, so this SM's L1 may hold stale lines
+    auto ld = [&](int p) -> C { return __ldcg(in + ib + p * ies); };
+    auto st = [&](int p, C v){ out[ob + p * oes] = do_scale ? cscale(v, scale) : v; };
+    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+}
+
 template<typename T, int EMAX, bool FWD, bool COLS>
 __global__ void __launch_bounds__(512)
 k_c2c(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
       long long G, int TPB, T scale, int do_scale){
-    using C = c_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
-    C *sm = reinterpret_cast<C*>(smraw);
-    int loc, t;
-    thread_map<COLS>(TPB, P.T, loc, t);
-    long long g = (long long)blockIdx.x * TPB + loc;
-    bool active = (g < G) && (t < P.T);
-    long long ib = active ? base_of(Li, g) : 0, ob = active ? base_of(Lo, g) : 0;
-    long long ies = Li.estride, oes = Lo.estride;
-    auto ld = [&](int p) -> C { return in[ib + p * ies]; };
-    auto st = [&](int p, C v){ out[ob + p * oes] = do_scale ? cscale(v, scale) : v; };
-    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+    tile_c2c<T, EMAX, FWD, COLS>(P, Li, Lo, in, out, tw, G, TPB, scale, do_scale, blockIdx.x,
+                                 reinterpret_cast<c_t<T>*>(smraw));
 }
 
 // ---------------------------------------------------------------------------
@@ -148,22 +160,20 @@ k_c2c(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> cons
 // Li is in real elements, Lo in complex elements; outputs k = 0..N/2.
 // ---------------------------------------------------------------------------
 template<typename T, int EMAX, bool COLS>
-__global__ void __launch_bounds__(512)
-k_r2c(Plan1D P, Layout Li, Layout Lo, T const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
-      long long G, int TPB, T scale, int do_scale){
+__device__ __forceinline__ void tile_r2c(Plan1D const &P, Layout Li, Layout Lo, T const *in, c_t<T> *out,
+                                         c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
+                                         long long tile, c_t<T> *sm){
     using C = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    C *sm = reinterpret_cast<C*>(smraw);
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
-    long long gp = (long long)blockIdx.x * TPB + loc;
+    long long gp = tile * TPB + loc;
     long long ga = 2 * gp, gb = 2 * gp + 1;
-    bool active = (ga < G) && (t < P.T);
+    bool active = (ga < G) && (t < P.T) && (loc < TPB);
     bool hasb = gb < G;
     long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
     long long ies = Li.estride;
     auto ld = [&](int p) -> C {
-        C z; z.x = in[ia + p * ies]; z.y = hasb ? in[ibb + p * ies] : (T)0; return z;
+        C z; z.x = __ldcg(in + ia + p * ies); z.y = hasb ? __ldcg(in + ibb + p * ies) : (T)0; return z;
     };
     auto st = [&](int, C){};
     int padn = padded_len(P.N);
@@ -187,23 +197,30 @@ k_r2c(Plan1D P, Layout Li, Layout Lo, T const *in, c_t<T> *out, c_t<T> const *__
     }
 }
 
+template<typename T, int EMAX, bool COLS>
+__global__ void __launch_bounds__(512)
+k_r2c(Plan1D P, Layout Li, Layout Lo, T const *in, c_t<T> *out, c_t<T> const *__restrict__ tw,
+      long long G, int TPB, T scale, int do_scale){
+    extern __shared__ __align__(16) unsigned char smraw[];
+    tile_r2c<T, EMAX, COLS>(P, Li, Lo, in, out, tw, G, TPB, scale, do_scale, blockIdx.x,
+                            reinterpret_cast<c_t<T>*>(smraw));
+}
+
 // ---------------------------------------------------------------------------
 // complex-to-real (unnormalised inverse): two half spectra in one complex FFT.
 // Z_p = X'_a[p] + i X'_b[p] with X'[p] = X[p] (p <= N/2, imaginary part of
 // the DC and Nyquist terms dropped) and conj X[N-p] above N/2.
 // ---------------------------------------------------------------------------
 template<typename T, int EMAX, bool COLS>
-__global__ void __launch_bounds__(512)
-k_c2r(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, T *out, c_t<T> const *__restrict__ tw,
-      long long G, int TPB, T scale, int do_scale){
+__device__ __forceinline__ void tile_c2r(Plan1D const &P, Layout Li, Layout Lo, c_t<T> const *in, T *out,
+                                         c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
+                                         long long tile, c_t<T> *sm){
     using C = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    C *sm = reinterpret_cast<C*>(smraw);
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
-    long long gp = (long long)blockIdx.x * TPB + loc;
+    long long gp = tile * TPB + loc;
     long long ga = 2 * gp, gb = 2 * gp + 1;
-    bool active = (ga < G) && (t < P.T);
+    bool active = (ga < G) && (t < P.T) && (loc < TPB);
     bool hasb = gb < G;
     long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
     long long oa = active ? base_of(Lo, ga) : 0, obb = (active && hasb) ? base_of(Lo, gb) : 0;
@@ -213,8 +230,8 @@ k_c2r(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, T *out, c_t<T> const *__
         int pp = (2 * p <= N) ? p : N - p;
         bool cj = (2 * p > N);
         bool real_only = (pp == 0) || (2 * pp == N);
-        C xa = in[ia + pp * ies];
-        C xb = hasb ? in[ibb + pp * ies] : mk<T>(0, 0);
+        C xa = __ldcg(in + ia + pp * ies);
+        C xb = hasb ? __ldcg(in + ibb + pp * ies) : mk<T>(0, 0);
         if (real_only){ xa.y = 0; xb.y = 0; }
         if (cj){ xa.y = -xa.y; xb.y = -xb.y; }
         C z; z.x = xa.x - xb.y; z.y = xa.y + xb.x; return z;
@@ -225,6 +242,15 @@ k_c2r(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, T *out, c_t<T> const *__
         if (hasb) out[obb + p * oes] = v.y * s;
     };
     fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+}
+
+template<typename T, int EMAX, bool COLS>
+__global__ void __launch_bounds__(512)
+k_c2r(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, T *out, c_t<T> const *__restrict__ tw,
+      long long G, int TPB, T scale, int do_scale){
+    extern __shared__ __align__(16) unsigned char smraw[];
+    tile_c2r<T, EMAX, COLS>(P, Li, Lo, in, out, tw, G, TPB, scale, do_scale, blockIdx.x,
+                            reinterpret_cast<c_t<T>*>(smraw));
 }
 
 // ---------------------------------------------------------------------------
@@ -248,7 +274,7 @@ k_r2r(Plan1D P, Layout Li, Layout Lo, T const *in, T *out, c_t<T> const *__restr
     thread_map<COLS>(TPB, P.T, loc, t);
     long long gp = (long long)blockIdx.x * TPB + loc;
     long long ga = 2 * gp, gb = 2 * gp + 1;
-    bool active = (ga < G) && (t < P.T);
+    bool active = (ga < G) && (t < P.T) && (loc < TPB);
     bool hasb = gb < G;
     long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
     long long oa = active ? base_of(Lo, ga) : 0, obb = (active && hasb) ? base_of(Lo, gb) : 0;

@@ -226,6 +226,49 @@ int heffte_gb300_forward_batch(heffte_gb300_plan plan, int batch, int prec, cons
 int heffte_gb300_backward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
                                 void *workspace, int scale);
 
+/* ======================================================================= */
+/* 4. Batches of many small boxes of uneven sizes, autotuner                */
+/* ======================================================================= */
+
+/* No reference counterpart as one call: it replaces a loop over many
+ * fft3d_r2c<cufft> (or fft3d<cufft>) objects, one per box, each box on one
+ * rank with order (0,1,2), r2c along dimension 0.  All boxes run in ONE
+ * persistent kernel launch (a device work queue over the 1-D passes of all
+ * boxes, with per-box pass dependencies), replayed as a CUDA graph.  Inputs
+ * of all boxes are packed in one array (box i at input_offset(i)), outputs in
+ * another (box i at output_offset(i)); offsets count elements of the
+ * respective type.  kind: HEFFTE_GB300_R2C or HEFFTE_GB300_C2C; sizes holds
+ * nboxes triplets (n0, n1, n2).  The backward transform needs a workspace of
+ * workspace_size() complex elements and leaves its input untouched; scaling
+ * is per box (1/(n0 n1 n2) for scale::full). */
+typedef struct heffte_gb300_boxbatch_s *heffte_gb300_boxbatch;
+int heffte_gb300_boxbatch_create(int kind, int prec, int nboxes, const int *sizes, void *stream,
+                                 heffte_gb300_boxbatch *batch);
+int heffte_gb300_boxbatch_destroy(heffte_gb300_boxbatch batch);
+long long heffte_gb300_boxbatch_input_offset(heffte_gb300_boxbatch batch, int box);
+long long heffte_gb300_boxbatch_output_offset(heffte_gb300_boxbatch batch, int box);
+long long heffte_gb300_boxbatch_input_size(heffte_gb300_boxbatch batch);
+long long heffte_gb300_boxbatch_output_size(heffte_gb300_boxbatch batch);
+long long heffte_gb300_boxbatch_workspace_size(heffte_gb300_boxbatch batch);
+int heffte_gb300_boxbatch_forward(heffte_gb300_boxbatch batch, const void *input, void *output, int scale);
+int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *input, void *output, void *workspace,
+                                   int scale);
+
+/* No reference counterpart.  Measures, on the current device, every candidate
+ * radix plan and tile size of each length and keeps the fastest for later
+ * batches (plans made after the call use it).  With a cache path the results
+ * are appended to that file after each length, keyed by the device, and
+ * lengths already in the file are not measured again (an interrupted tuning
+ * resumes).  *measured (may be NULL) receives the number of lengths timed. */
+int heffte_gb300_tune(int prec, int nlengths, const int *lengths, const char *cache_path, void *stream,
+                      int *measured);
+/* Loads the entries of a tuning cache written for this device. */
+int heffte_gb300_tune_load(const char *cache_path, int *entries);
+int heffte_gb300_tune_clear(void);
+/* The tuned choice of a length (nradices = 0 when it was never measured);
+ * radices must hold 16 ints. */
+int heffte_gb300_tuned_choice(int prec, int length, int *radices, int *nradices, int *tpb, double *us);
+
 #ifdef __cplusplus
 }
 #endif
