@@ -211,7 +211,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
                 U.Li = pass_layout(sb, d, {0, 1, 2});
                 U.Lo = pass_layout(db, d, {0, 1, 2});
                 U.cols = (d != 0);
-                U.G = rbox.count() / rbox.size[d];
+                U.G = sb.count() / sb.size[d];      // transforms of the box this pass reads
                 U.plan = plan_of[(int)rbox.size[d]];
                 Fft1D const &f = *b->ffts[U.plan];
                 bool paired = is_r2x;
@@ -258,6 +258,25 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     std::vector<BatchUnit> fu, bu;
     build(true, fu, b->fwd_tiles);
     build(false, bu, b->bwd_tiles);
+    // every element a unit touches must lie inside its buffer (checked on the host)
+    auto last_elem = [](Layout const &L, long long G, long long N){
+        long long blocks = (G + L.count - 1) / L.count;
+        return (blocks - 1) * L.bstride + (std::min(G, L.count) - 1) * L.dist + (N - 1) * L.estride;
+    };
+    for (auto const *v : {&fu, &bu}){
+        bool fwd = (v == &fu);
+        for (auto const &U : *v){
+            long long N = b->ffts[U.plan]->N;
+            // forward: input (in_total) -> output (out_total); backward: input
+            // and workspace hold half spectra (out_total), the output the boxes (in_total)
+            long long in_cap = (fwd && U.src == 0) ? b->in_total : b->out_total;
+            long long out_cap = (!fwd && U.dst == 1) ? b->in_total : b->out_total;
+            long long in_len = (U.kind == K_C2R) ? N / 2 + 1 : N;
+            long long out_len = (U.kind == K_R2C) ? N / 2 + 1 : N;
+            if (U.in_off + last_elem(U.Li, U.G, in_len) >= in_cap || U.out_off + last_elem(U.Lo, U.G, out_len) >= out_cap)
+                throw Error(ST_INVALID, "internal error: batch unit exceeds its buffer");
+        }
+    }
     b->nunits = (int)fu.size();
     // device tables
     auto dalloc = [&](size_t bytes) -> void* {
