@@ -319,6 +319,8 @@ WORKLOADS = {
     "batch256": ("batch", None, 0),
     # the same after autotuning the radix plan / tile size of every side length
     "batch256tuned": ("batch", "tuned", 0),
+    # the same boxes as a loop over one fft3d_r2c plan per box (how the reference runs them)
+    "batch256loop": ("batch", "loop", 0),
 }
 
 BATCH_SIDES = [16, 24, 32, 40, 48, 64, 80, 96, 128]
@@ -329,11 +331,51 @@ def batch_sizes(nboxes=256, seed=256):
     return [tuple(int(v) for v in rng.choice(BATCH_SIDES, 3)) for _ in range(nboxes)]
 
 
+def run_batch_loop(name, sizes, steps, warmup):
+    import torch
+    import heffte_gb300 as gb
+    stream = torch.cuda.current_stream()
+    plans, xs, ys, zs = [], [], [], []
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    for s in sizes:
+        box = gb.box3d((0, 0, 0), [v - 1 for v in s])
+        p = gb.fft3d_r2c(box, box.r2c(0), 0, stream=stream)
+        plans.append(p)
+        xs.append(torch.randn(p.size_inbox(), device="cuda", generator=gen))
+        ys.append(torch.empty(p.size_outbox(), dtype=torch.complex64, device="cuda"))
+        zs.append(torch.empty(p.size_inbox(), device="cuda"))
+
+    def step():
+        for p, x, y, z in zip(plans, xs, ys, zs):
+            p.forward(x, y, gb.scale.full)
+            p.backward(y, z, gb.scale.none)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    flops = sum(2 * flops_per_transform(s[0] * s[1] * s[2]) for s in sizes)
+    byts = sum(2 * algorithmic_bytes("r2c", s, 0) for s in sizes)
+    peak, _ = peaks()
+    return {"workload": name, "boxes": len(sizes), "ms_per_step": ms, "gflops": flops / (ms / 1e3) / 1e9,
+            "gbs": byts / (ms / 1e3) / 1e9, "hbm_frac": byts / (ms / 1e3) / 1e9 / peak,
+            "launches_per_step": 6 * len(sizes)}
+
+
 def run_batch_workload(name, steps, warmup, tune_cache=None):
     import torch
     import heffte_gb300 as gb
     sizes = batch_sizes()
     stream = torch.cuda.current_stream()
+    if tune_cache == "loop":
+        return run_batch_loop(name, sizes, steps, warmup)
     if tune_cache is not None:
         gb.tune(0, BATCH_SIDES, tune_cache, stream=stream)
     b = gb.boxbatch(gb.kind.r2c, sizes, 0, stream=stream)
@@ -384,7 +426,7 @@ def run_workload(name, steps, warmup):
     import heffte_gb300 as gb
     kind, size, prec = WORKLOADS[name]
     if kind == "batch":
-        cache = None
+        cache = "loop" if size == "loop" else None
         if size == "tuned":
             import tempfile
             cache = os.path.join(tempfile.mkdtemp(), "tune.tsv")

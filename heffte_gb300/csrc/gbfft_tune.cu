@@ -2,9 +2,10 @@
 // (runtime-radix) kernels, used by the batched multi-box path.
 //
 // For a length N every candidate radix plan (ordered factorisations into the
-// supported radices, at most four stages) and two tile sizes are timed with
-// CUDA events on two probes that stand for the two pass shapes of a box
-// (contiguous lines and strided columns); the fastest is kept.  Results live
+// supported radices, at most four stages) is timed with CUDA events inside the
+// batched kernel itself (a batch of N^3 boxes, r2c forward + backward, the
+// tile of 256 threads / T transforms that kernel uses); the fastest is kept.
+// Results live
 // in a process-wide table and, when a cache path is given, are appended to a
 // tab-separated file after every length, keyed by the device (name, SM count,
 // driver and library versions): a later run loads the file and skips what was
@@ -104,19 +105,16 @@ int tune_load(std::string const &path){
     return n;
 }
 
-static double time_candidate(cudaStream_t s, Fft1D &f, int prec, int tpb, void *buf, void *buf2, long long G){
-    Layout lines{G, f.N, (long long)G * f.N, 1};
-    Layout cols{G, 1, (long long)G, G};
-    LaunchCfg cfg;
-    cfg.variant = 1;
-    cfg.tpb = tpb;
+// Times one candidate inside the batched kernel it is tuned for: a batch of
+// boxes whose three sides are all N (the batch reads the candidate from the
+// table), r2c forward + backward.
+static double time_in_batch(cudaStream_t s, int N, int prec, void *in, void *out, void *work, int nbox){
+    std::vector<std::array<int, 3>> sizes(nbox, std::array<int, 3>{N, N, N});
+    auto b = make_batch(PK_R2C, prec, sizes, s);
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");
-    auto once = [&]{
-        launch_c2c(s, f, prec, true, lines, lines, buf, buf2, G, 1.0, cfg);
-        launch_c2c(s, f, prec, true, cols, cols, buf2, buf, G, 1.0, cfg);
-    };
+    auto once = [&]{ b->run(true, in, out, nullptr, 0); b->run(false, out, in, work, 0); };
     once();
     once();
     const int reps = 5;
@@ -142,25 +140,32 @@ int tune_lengths(std::vector<int> const &lengths, int prec, cudaStream_t s, std:
             if (g_table.count({prec, N})) continue;
         }
         if (!supported_length(N, prec) || N < 2) continue;
-        long long G = std::max<long long>(256, (1LL << 21) / N);
-        void *buf = nullptr, *buf2 = nullptr;
-        check_cuda(cudaMalloc(&buf, (size_t)G * N * csize), "cudaMalloc(tuning buffer)");
-        check_cuda(cudaMalloc(&buf2, (size_t)G * N * csize), "cudaMalloc(tuning buffer)");
-        check_cuda(cudaMemsetAsync(buf, 0, (size_t)G * N * csize, s), "memset");
+        // boxes of N^3, enough of them for about 2^24 values per batch
+        long long per = (long long)N * N * N;
+        int nbox = (int)std::max<long long>(1, std::min<long long>(64, (1LL << 24) / per));
+        size_t elems = (size_t)per * nbox;
+        void *in = nullptr, *out = nullptr, *work = nullptr;
+        check_cuda(cudaMalloc(&in, elems * csize), "cudaMalloc(tuning buffer)");
+        check_cuda(cudaMalloc(&out, elems * csize), "cudaMalloc(tuning buffer)");
+        check_cuda(cudaMalloc(&work, elems * csize), "cudaMalloc(tuning buffer)");
+        check_cuda(cudaMemsetAsync(in, 0, elems * csize, s), "memset");
         TuneChoice best;
         best.us = 1e30;
         for (auto const &rad : radix_candidates(N)){
             std::shared_ptr<Fft1D> f;
             try { f = get_fft1d(N, rad); } catch (Error const &){ continue; }
-            if (f->plan.T > 512) continue;
+            if (f->plan.T > 256) continue;
             int deft = std::max(1, 256 / f->plan.T);
-            for (int tpb : {deft, std::max(1, deft / 2)}){
-                double us = time_candidate(s, *f, prec, tpb, buf, buf2, G);
-                if (us < best.us){ best.us = us; best.radices = rad; best.tpb = tpb; }
+            {
+                std::lock_guard<std::mutex> lk(g_mu);
+                g_table[{prec, N}] = TuneChoice{rad, deft, 0};
             }
+            double us = time_in_batch(s, N, prec, in, out, work, nbox);
+            if (us < best.us){ best.us = us; best.radices = rad; best.tpb = deft; }
         }
-        cudaFree(buf);
-        cudaFree(buf2);
+        cudaFree(in);
+        cudaFree(out);
+        cudaFree(work);
         {
             std::lock_guard<std::mutex> lk(g_mu);
             g_table[{prec, N}] = best;
