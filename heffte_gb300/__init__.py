@@ -92,6 +92,20 @@ def lib():
     L.heffte_gb300_tune_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
     L.heffte_gb300_tuned_choice.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    ip, fp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
+    L.heffte_gb300_plan_set_knobs.argtypes = [vp, i, i, i]
+    L.heffte_gb300_plan_features.argtypes = [i, i, I3, fp]
+    L.heffte_gb300_candidate_options.argtypes = [i, vp, ip, ip, ip]
+    L.heffte_gb300_mlp_create.argtypes = [i, i, i, ctypes.c_ulonglong, ctypes.POINTER(vp)]
+    L.heffte_gb300_mlp_destroy.argtypes = [vp]
+    L.heffte_gb300_mlp_num_params.argtypes = [vp]
+    L.heffte_gb300_mlp_num_params.restype = ll
+    L.heffte_gb300_mlp_get_params.argtypes = [vp, fp]
+    L.heffte_gb300_mlp_set_params.argtypes = [vp, fp]
+    L.heffte_gb300_mlp_loss_grad.argtypes = [vp, vp, vp, i, fp, fp]
+    L.heffte_gb300_mlp_train.argtypes = [vp, vp, vp, i, i, ctypes.c_float, vp, fp]
+    L.heffte_gb300_mlp_predict.argtypes = [vp, vp, vp, i, vp]
+    L.heffte_gb300_select.argtypes = [vp, i, i, I3, ip]
     _lib = L
     return L
 
@@ -202,6 +216,10 @@ class _plan:
     def set_stream(self, stream):
         self.stream = _stream_handle(stream)
         check(lib().heffte_gb300_plan_set_stream(self._h, self.stream))
+
+    def set_knobs(self, variant=0, tile_div=1, radix_policy=0):
+        """Re-plans with a kernel family (0 pipelined, 1 one-shot), tile divisor (1, 2) and radix order (0, 1)."""
+        check(lib().heffte_gb300_plan_set_knobs(self._h, variant, tile_div, radix_policy))
 
     def size_inbox(self):
         return lib().heffte_gb300_size_inbox(self._h)

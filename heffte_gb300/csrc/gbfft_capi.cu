@@ -1,6 +1,7 @@
 // extern "C" boundary of libheffte_gb300 (declarations in include/heffte_gb300.h).
 #include "gbfft_plan.h"
 #include "gbfft_batch.h"
+#include "gbfft_mlp.h"
 #include "../../include/heffte_gb300.h"
 #include <cstring>
 #include <new>
@@ -342,6 +343,112 @@ int heffte_gb300_tune_load(const char *cache_path, int *entries){
 }
 
 int heffte_gb300_tune_clear(void){ return guard([&]{ tune_clear(); }); }
+
+// ---------------------------------------------------------------------------
+// plan knobs and the learned selector
+// ---------------------------------------------------------------------------
+int heffte_gb300_plan_set_knobs(heffte_gb300_plan plan, int variant, int tile_div, int radix_policy){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan");
+        if (variant < 0 || variant > 1 || (tile_div != 1 && tile_div != 2) || radix_policy < 0 || radix_policy > 1)
+            throw Error(ST_INVALID, "invalid knobs");
+        Plan3D &p = *plan->p;
+        Knobs k;
+        k.variant = variant; k.tile_div = tile_div; k.radix_policy = radix_policy;
+        plan->p = make_plan(p.kind, p.inbox, p.outbox, p.r2c_dir, p.opts, p.stream, k);
+    });
+}
+
+int heffte_gb300_plan_features(int kind, int prec, const int size[3], float *features){
+    return guard([&]{
+        if (!size || !features) throw Error(ST_INVALID, "null pointer");
+        plan_features(kind, prec, size, features);
+    });
+}
+
+int heffte_gb300_candidate_options(int candidate, heffte_gb300_plan_options *options, int *variant, int *tile_div,
+                                   int *radix_policy){
+    return guard([&]{
+        if (candidate < 0 || candidate >= kCandidates) throw Error(ST_INVALID, "candidate out of range");
+        Options o; Knobs k;
+        candidate_knobs(candidate, o, k);
+        if (options){ options->use_reorder = o.use_reorder; options->algorithm = 0; options->use_pencils = 1; options->use_gpu_aware = 1; }
+        if (variant) *variant = k.variant;
+        if (tile_div) *tile_div = k.tile_div;
+        if (radix_policy) *radix_policy = k.radix_policy;
+    });
+}
+
+struct heffte_gb300_mlp_s { std::unique_ptr<Mlp> m; };
+
+int heffte_gb300_mlp_create(int nin, int nhidden, int nout, unsigned long long seed, heffte_gb300_mlp *out){
+    return guard([&]{
+        if (!out) throw Error(ST_INVALID, "null pointer");
+        *out = nullptr;
+        auto *h = new heffte_gb300_mlp_s;
+        try { h->m = std::make_unique<Mlp>(nin, nhidden, nout, seed); } catch (...) { delete h; throw; }
+        *out = h;
+    });
+}
+int heffte_gb300_mlp_destroy(heffte_gb300_mlp m){ return guard([&]{ delete m; }); }
+long long heffte_gb300_mlp_num_params(heffte_gb300_mlp m){ return m ? m->m->nparams : -1; }
+
+int heffte_gb300_mlp_get_params(heffte_gb300_mlp m, float *host){
+    return guard([&]{
+        if (!m || !host) throw Error(ST_INVALID, "null pointer");
+        check_cuda(cudaMemcpy(host, m->m->params, m->m->nparams * sizeof(float), cudaMemcpyDeviceToHost), "copy params");
+    });
+}
+int heffte_gb300_mlp_set_params(heffte_gb300_mlp m, const float *host){
+    return guard([&]{
+        if (!m || !host) throw Error(ST_INVALID, "null pointer");
+        check_cuda(cudaMemcpy(m->m->params, host, m->m->nparams * sizeof(float), cudaMemcpyHostToDevice), "copy params");
+    });
+}
+
+int heffte_gb300_mlp_loss_grad(heffte_gb300_mlp m, const float *X, const float *T, int n, float *loss, float *host_grads){
+    return guard([&]{
+        if (!m || !X || !T || n < 1) throw Error(ST_INVALID, "invalid arguments");
+        m->m->loss_and_grad(nullptr, X, T, n);
+        check_cuda(cudaDeviceSynchronize(), "mlp gradient");
+        if (loss) check_cuda(cudaMemcpy(loss, m->m->loss_d, sizeof(float), cudaMemcpyDeviceToHost), "copy loss");
+        if (host_grads) check_cuda(cudaMemcpy(host_grads, m->m->grads, m->m->nparams * sizeof(float), cudaMemcpyDeviceToHost), "copy grads");
+    });
+}
+
+int heffte_gb300_mlp_train(heffte_gb300_mlp m, const float *X, const float *T, int n, int steps, float lr, void *stream,
+                           float *final_loss){
+    return guard([&]{
+        if (!m || !X || !T || n < 1 || steps < 0) throw Error(ST_INVALID, "invalid arguments");
+        float l = m->m->train(as_stream(stream), X, T, n, steps, lr);
+        if (final_loss) *final_loss = l;
+    });
+}
+
+int heffte_gb300_mlp_predict(heffte_gb300_mlp m, const float *X, float *Y, int n, void *stream){
+    return guard([&]{
+        if (!m || !X || !Y || n < 1) throw Error(ST_INVALID, "invalid arguments");
+        m->m->forward(as_stream(stream), X, n);
+        check_cuda(cudaMemcpyAsync(Y, m->m->y, (size_t)n * m->m->nout * sizeof(float), cudaMemcpyDeviceToDevice,
+                                   as_stream(stream)), "copy predictions");
+    });
+}
+
+int heffte_gb300_select(heffte_gb300_mlp m, int kind, int prec, const int size[3], int *candidate){
+    return guard([&]{
+        if (!m || !size || !candidate) throw Error(ST_INVALID, "null pointer");
+        if (m->m->nin != kFeatures || m->m->nout != kCandidates) throw Error(ST_INVALID, "the network does not match the selector's features / candidates");
+        float f[kFeatures];
+        plan_features(kind, prec, size, f);
+        check_cuda(cudaMemcpy(m->m->xrow, f, sizeof(f), cudaMemcpyHostToDevice), "copy features");
+        m->m->forward(nullptr, m->m->xrow, 1);
+        float y[kCandidates];
+        check_cuda(cudaMemcpy(y, m->m->y, sizeof(y), cudaMemcpyDeviceToHost), "copy prediction");
+        int best = 0;
+        for (int c = 1; c < kCandidates; c++) if (y[c] < y[best]) best = c;
+        *candidate = best;
+    });
+}
 
 int heffte_gb300_tuned_choice(int prec, int length, int *radices, int *nradices, int *tpb, double *us){
     return guard([&]{

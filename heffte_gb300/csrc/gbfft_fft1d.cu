@@ -195,6 +195,7 @@ static void geometry(Fft1D &f, int prec, bool cols, bool paired, long long G, La
     else if (cols) tpb = std::max((prec == 0) ? (paired ? 16 : 16) : 8, (256 + T - 1) / T);
     else tpb = std::max(1, 256 / T);
     tpb = std::min(tpb, std::max(1, 512 / T));
+    if (cfg.tpb <= 0 && cfg.tpb_div > 1) tpb = std::max(1, tpb / cfg.tpb_div);
     size_t budget = 100 * 1024;
     while (tpb > 1 && (size_t)tpb * unit > budget) tpb--;
     if ((size_t)tpb * unit > 227 * 1024) throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(N) + " does not fit in shared memory");

@@ -61,6 +61,7 @@ int max_length(int prec);
 struct LaunchCfg {
     int tpb = 0;      // transforms (or transform pairs) per CTA; 0 = automatic
     int variant = 0;  // 0 = process-wide choice, 1 = generic kernels, 2 = pipelined kernels
+    int tpb_div = 1;  // divides the automatic tile of the generic kernels
 };
 
 // Batched 1-D launches (in units of elements of the respective arrays).

@@ -93,6 +93,15 @@ void Executor::backward(cudaStream_t s, int prec, void const *in, void *out, dou
     }
 }
 
+std::shared_ptr<Fft1D> fft_for(int N, int radix_policy){
+    if (radix_policy == 1){
+        std::vector<int> r = default_radices(N);
+        std::sort(r.begin(), r.end());
+        if (!r.empty()) return get_fft1d(N, r);
+    }
+    return get_fft1d(N);
+}
+
 // ---------------------------------------------------------------------------
 // plan construction
 // ---------------------------------------------------------------------------
@@ -119,7 +128,7 @@ std::array<int, 3> order_with_first(std::array<int, 3> const &cur, int d){
 //   out_holds_inter: the output buffer has the element type of the intermediate data
 std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_box, Box3 const &dst_box,
                           Box3 const &inter_geom, bool reorder, bool out_holds_inter, bool in_aliases_out,
-                          int &work_buffers){
+                          int &work_buffers, int radix_policy){
     // drop length-1 complex passes (identity), keep at least one op to move
     // the data; a length-1 r2r transform is not the identity (REDFT10 of one
     // value is twice the value) and r2c/c2r change the element type
@@ -154,7 +163,8 @@ std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_b
         }
         f.dbox = next;
         f.ref_order = cur.order;
-        f.fft = get_fft1d((int)((p.kind == K_R2C) ? cur.size[p.dim] : (p.kind == K_C2R ? dst_box.size[p.dim] : cur.size[p.dim])));
+        f.fft = fft_for((int)((p.kind == K_R2C) ? cur.size[p.dim] : (p.kind == K_C2R ? dst_box.size[p.dim] : cur.size[p.dim])),
+                        radix_policy);
         ops.push_back(f);
         cur = next;
     }
@@ -217,7 +227,7 @@ std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_b
 } // namespace
 
 std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbox, int r2c_dir, Options const &o,
-                                  cudaStream_t stream){
+                                  cudaStream_t stream, Knobs const &knobs){
     if (!valid_order(inbox.order) || !valid_order(outbox.order)) throw Error(ST_INVALID, "invalid box order");
     if (inbox.empty()) throw Error(ST_INVALID, "empty input box");
     auto p = std::make_unique<Plan3D>();
@@ -226,6 +236,7 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
     p->r2c_dir = r2c_dir;
     p->opts = o;
     p->stream = stream;
+    p->knobs = knobs;
     // single rank: the boxes are the whole world (heffte_fft3d.h:270-297 on MPI_COMM_SELF)
     if (kind == PK_R2C){
         if (r2c_dir < 0 || r2c_dir > 2) throw Error(ST_INVALID, "r2c_direction must be 0, 1 or 2");
@@ -252,9 +263,9 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         std::vector<PassSpec> fwd, bwd;
         for (int i = 0; i < 3; i++) fwd.push_back({r2r ? K_R2R_F : K_C2C_F, io[i]});
         for (int i = 0; i < 3; i++) bwd.push_back({r2r ? K_R2R_B : K_C2C_B, oo[i]});
-        p->fwd = build_ops(fwd, inbox, outbox, inbox, reorder, true, false, wf);
+        p->fwd = build_ops(fwd, inbox, outbox, inbox, reorder, true, false, wf, knobs.radix_policy);
         p->fwd_alias = p->fwd;
-        p->bwd = build_ops(bwd, outbox, inbox, inbox, reorder, true, false, wb);
+        p->bwd = build_ops(bwd, outbox, inbox, inbox, reorder, true, false, wb, knobs.radix_policy);
         p->work_elems = std::max(wf, wb) * inbox.count();
         double n = (double)inbox.count();
         p->scale_factor = r2r ? 1.0 / (64.0 * n) : 1.0 / n;
@@ -264,9 +275,9 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         for (int i = 0; i < 3; i++) if (io[i] != r2c_dir) fwd.push_back({K_C2C_F, io[i]});
         for (int i = 0; i < 3; i++) if (oo[i] != r2c_dir) bwd.push_back({K_C2C_B, oo[i]});
         bwd.push_back({K_C2R, r2c_dir});
-        p->fwd = build_ops(fwd, inbox, outbox, cgeom, reorder, true, false, wf);
-        p->fwd_alias = build_ops(fwd, inbox, outbox, cgeom, reorder, true, true, wfa);
-        p->bwd = build_ops(bwd, outbox, inbox, cgeom, reorder, false, false, wb);
+        p->fwd = build_ops(fwd, inbox, outbox, cgeom, reorder, true, false, wf, knobs.radix_policy);
+        p->fwd_alias = build_ops(fwd, inbox, outbox, cgeom, reorder, true, true, wfa, knobs.radix_policy);
+        p->bwd = build_ops(bwd, outbox, inbox, cgeom, reorder, false, false, wb, knobs.radix_policy);
         p->work_elems = std::max(std::max(wf, wfa), wb) * cgeom.count();
         p->scale_factor = 1.0 / (double)inbox.count();
     }
@@ -319,6 +330,9 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
         wbase = reinterpret_cast<char*>(cached_work);
     }
     double sc = get_scale(scaling);
+    LaunchCfg cfg;
+    cfg.variant = (knobs.variant == 1) ? 1 : 0;
+    cfg.tpb_div = std::max(1, knobs.tile_div);
     for (int j = 0; j < batch; j++){
         void *bufs[4];
         bufs[0] = const_cast<char*>(reinterpret_cast<char const*>(in)) + (size_t)j * in_cnt * in_es;
@@ -334,12 +348,12 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
                 Layout Lo = pass_layout(op.dbox, op.dim, op.ref_order);
                 long long G = op.sbox.count() / op.sbox.size[op.dim];
                 switch (op.kind){
-                    case K_C2C_F: launch_c2c(stream, *op.fft, prec, true, Li, Lo, src, dst, G, s); break;
-                    case K_C2C_B: launch_c2c(stream, *op.fft, prec, false, Li, Lo, src, dst, G, s); break;
-                    case K_R2C: launch_r2c(stream, *op.fft, prec, Li, Lo, src, dst, G, s); break;
-                    case K_C2R: launch_c2r(stream, *op.fft, prec, Li, Lo, src, dst, G, s); break;
-                    case K_R2R_F: launch_r2r(stream, *op.fft, prec, true, kind == PK_SIN, Li, Lo, src, dst, G, s); break;
-                    case K_R2R_B: launch_r2r(stream, *op.fft, prec, false, kind == PK_SIN, Li, Lo, src, dst, G, s); break;
+                    case K_C2C_F: launch_c2c(stream, *op.fft, prec, true, Li, Lo, src, dst, G, s, cfg); break;
+                    case K_C2C_B: launch_c2c(stream, *op.fft, prec, false, Li, Lo, src, dst, G, s, cfg); break;
+                    case K_R2C: launch_r2c(stream, *op.fft, prec, Li, Lo, src, dst, G, s, cfg); break;
+                    case K_C2R: launch_c2r(stream, *op.fft, prec, Li, Lo, src, dst, G, s, cfg); break;
+                    case K_R2R_F: launch_r2r(stream, *op.fft, prec, true, kind == PK_SIN, Li, Lo, src, dst, G, s, cfg); break;
+                    case K_R2R_B: launch_r2r(stream, *op.fft, prec, false, kind == PK_SIN, Li, Lo, src, dst, G, s, cfg); break;
                 }
             } else if (op.type == Op::RESHAPE){
                 Box3 const &A = op.sbox, &B = op.dbox;

@@ -71,6 +71,16 @@ struct Options {
 
 enum PlanKind { PK_C2C = 0, PK_R2C = 1, PK_COS = 2, PK_SIN = 3 };
 
+// Tuning knobs of a plan (the choices the learned selector makes): kernel
+// family (0 pipelined where it applies, 1 generic only), tile of the generic
+// kernels (automatic / tile_div), radix order (0 default, 1 ascending).
+struct Knobs {
+    int variant = 0;
+    int tile_div = 1;
+    int radix_policy = 0;
+};
+std::shared_ptr<Fft1D> fft_for(int N, int radix_policy);
+
 // One operation of a compiled plan.
 struct Op {
     enum Type { FFT, RESHAPE, COPY } type = FFT;
@@ -95,6 +105,7 @@ struct Plan3D {
     double scale_factor = 1.0;    // "full" factor
     void *cached_work = nullptr;  // lazily allocated when the caller passes no workspace
     size_t cached_bytes = 0;
+    Knobs knobs;
     ~Plan3D();
 
     long long size_inbox() const { return inbox.count(); }
@@ -105,6 +116,6 @@ struct Plan3D {
 };
 
 std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbox, int r2c_dir, Options const &o,
-                                  cudaStream_t stream);
+                                  cudaStream_t stream, Knobs const &knobs = Knobs{});
 
 } // namespace gbfft

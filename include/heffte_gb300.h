@@ -269,6 +269,44 @@ int heffte_gb300_tune_clear(void);
  * radices must hold 16 ints. */
 int heffte_gb300_tuned_choice(int prec, int length, int *radices, int *nradices, int *tpb, double *us);
 
+/* ======================================================================= */
+/* 5. Plan knobs and the learned plan selector (no reference counterpart)   */
+/* ======================================================================= */
+
+/* Re-plans with the given knobs: variant 0 = pipelined kernels where they
+ * apply, 1 = generic kernels only; tile_div 1 or 2 divides the automatic tile
+ * of the generic kernels; radix_policy 0 = default radix order, 1 = ascending.
+ * Results are unchanged (within rounding); only the speed differs. */
+int heffte_gb300_plan_set_knobs(heffte_gb300_plan plan, int variant, int tile_div, int radix_policy);
+/* The 18 features the selector reads for a transform of `kind` and `prec`. */
+int heffte_gb300_plan_features(int kind, int prec, const int size[3], float *features);
+/* Candidate c in [0, 16): use_reorder = c & 1, variant = (c >> 1) & 1,
+ * tile_div = 1 + ((c >> 2) & 1), radix_policy = (c >> 3) & 1. */
+int heffte_gb300_candidate_options(int candidate, heffte_gb300_plan_options *options, int *variant, int *tile_div,
+                                   int *radix_policy);
+
+/* A 3-layer perceptron (nin -> nhidden -> nhidden -> nout, ReLU), trained on
+ * the GPU by this library's own forward, backward and Adam kernels (FP32).
+ * Parameters are W1, b1, W2, b2, W3, b3 (row-major, W[in][out]).  X and T
+ * are device arrays of n rows; the loss is the mean squared error. */
+typedef struct heffte_gb300_mlp_s *heffte_gb300_mlp;
+int heffte_gb300_mlp_create(int nin, int nhidden, int nout, unsigned long long seed, heffte_gb300_mlp *mlp);
+int heffte_gb300_mlp_destroy(heffte_gb300_mlp mlp);
+long long heffte_gb300_mlp_num_params(heffte_gb300_mlp mlp);
+int heffte_gb300_mlp_get_params(heffte_gb300_mlp mlp, float *host_params);
+int heffte_gb300_mlp_set_params(heffte_gb300_mlp mlp, const float *host_params);
+/* Loss and gradient of one full batch (host copies; synchronises). */
+int heffte_gb300_mlp_loss_grad(heffte_gb300_mlp mlp, const float *X, const float *T, int n, float *loss,
+                               float *host_grads);
+/* `steps` full-batch Adam steps with learning rate lr; *final_loss = last loss. */
+int heffte_gb300_mlp_train(heffte_gb300_mlp mlp, const float *X, const float *T, int n, int steps, float lr,
+                           void *stream, float *final_loss);
+/* Y[n x nout] = network(X[n x nin]) (device arrays). */
+int heffte_gb300_mlp_predict(heffte_gb300_mlp mlp, const float *X, float *Y, int n, void *stream);
+/* The candidate the network predicts fastest for one transform (an
+ * 18-in / 16-out network); the caller then uses heffte_gb300_candidate_options. */
+int heffte_gb300_select(heffte_gb300_mlp mlp, int kind, int prec, const int size[3], int *candidate);
+
 #ifdef __cplusplus
 }
 #endif
