@@ -94,6 +94,7 @@ def lib():
                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     ip, fp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
     L.heffte_gb300_plan_set_knobs.argtypes = [vp, i, i, i]
+    L.heffte_gb300_plan_set_tensor_cores.argtypes = [vp, i]
     L.heffte_gb300_plan_features.argtypes = [i, i, I3, fp]
     L.heffte_gb300_candidate_options.argtypes = [i, vp, ip, ip, ip]
     L.heffte_gb300_mlp_create.argtypes = [i, i, i, ctypes.c_ulonglong, ctypes.POINTER(vp)]
@@ -220,6 +221,10 @@ class _plan:
     def set_knobs(self, variant=0, tile_div=1, radix_policy=0):
         """Re-plans with a kernel family (0 pipelined, 1 one-shot), tile divisor (1, 2) and radix order (0, 1)."""
         check(lib().heffte_gb300_plan_set_knobs(self._h, variant, tile_div, radix_policy))
+
+    def set_tensor_cores(self, enable=True):
+        """complex<float> radix-16 stages as split-BF16 DFT contractions on the tensor cores (or back to FP32)."""
+        check(lib().heffte_gb300_plan_set_tensor_cores(self._h, 1 if enable else 0))
 
     def size_inbox(self):
         return lib().heffte_gb300_size_inbox(self._h)

@@ -353,8 +353,19 @@ int heffte_gb300_plan_set_knobs(heffte_gb300_plan plan, int variant, int tile_di
         if (variant < 0 || variant > 1 || (tile_div != 1 && tile_div != 2) || radix_policy < 0 || radix_policy > 1)
             throw Error(ST_INVALID, "invalid knobs");
         Plan3D &p = *plan->p;
-        Knobs k;
+        Knobs k = p.knobs;
         k.variant = variant; k.tile_div = tile_div; k.radix_policy = radix_policy;
+        plan->p = make_plan(p.kind, p.inbox, p.outbox, p.r2c_dir, p.opts, p.stream, k);
+    });
+}
+
+int heffte_gb300_plan_set_tensor_cores(heffte_gb300_plan plan, int enable){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan");
+        if (enable != 0 && enable != 1) throw Error(ST_INVALID, "enable must be 0 or 1");
+        Plan3D &p = *plan->p;
+        Knobs k = p.knobs;
+        k.tensor_cores = enable;
         plan->p = make_plan(p.kind, p.inbox, p.outbox, p.r2c_dir, p.opts, p.stream, k);
     });
 }

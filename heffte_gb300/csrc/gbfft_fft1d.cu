@@ -340,6 +340,10 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
 void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (cfg.tc && prec == 0 && tc_supported(f.N)){
+        launch_tc_c2c(s, f.N, fwd, Li, Lo, in, out, G, scale);
+        return;
+    }
     if (try_pipe(s, fwd ? K_C2C_F : K_C2C_B, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);

@@ -62,7 +62,15 @@ struct LaunchCfg {
     int tpb = 0;      // transforms (or transform pairs) per CTA; 0 = automatic
     int variant = 0;  // 0 = process-wide choice, 1 = generic kernels, 2 = pipelined kernels
     int tpb_div = 1;  // divides the automatic tile of the generic kernels
+    int tc = 0;       // 1: complex<float> radix-16 stages on the tensor cores (split BF16)
 };
+
+// Tensor-core (tcgen05, split-BF16) complex<float> transforms of lengths
+// 16^s * {1, 2, 4, 8} in [64, 4096].
+bool tc_supported(int N);
+std::vector<int> tc_radices(int N);
+void launch_tc_c2c(cudaStream_t s, int N, bool fwd, Layout Li, Layout Lo, void const *in, void *out, long long G,
+                   double scale);
 
 // Batched 1-D launches (in units of elements of the respective arrays).
 void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,

@@ -333,6 +333,7 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
     LaunchCfg cfg;
     cfg.variant = (knobs.variant == 1) ? 1 : 0;
     cfg.tpb_div = std::max(1, knobs.tile_div);
+    cfg.tc = knobs.tensor_cores;
     for (int j = 0; j < batch; j++){
         void *bufs[4];
         bufs[0] = const_cast<char*>(reinterpret_cast<char const*>(in)) + (size_t)j * in_cnt * in_es;

@@ -73,11 +73,14 @@ enum PlanKind { PK_C2C = 0, PK_R2C = 1, PK_COS = 2, PK_SIN = 3 };
 
 // Tuning knobs of a plan (the choices the learned selector makes): kernel
 // family (0 pipelined where it applies, 1 generic only), tile of the generic
-// kernels (automatic / tile_div), radix order (0 default, 1 ascending).
+// kernels (automatic / tile_div), radix order (0 default, 1 ascending); and
+// the precision form of the complex<float> passes (tensor_cores = 1: radix-16
+// stages as split-BF16 DFT contractions on the tensor cores).
 struct Knobs {
     int variant = 0;
     int tile_div = 1;
     int radix_policy = 0;
+    int tensor_cores = 0;
 };
 std::shared_ptr<Fft1D> fft_for(int N, int radix_policy);
 

@@ -278,6 +278,14 @@ int heffte_gb300_tuned_choice(int prec, int length, int *radices, int *nradices,
  * of the generic kernels; radix_policy 0 = default radix order, 1 = ascending.
  * Results are unchanged (within rounding); only the speed differs. */
 int heffte_gb300_plan_set_knobs(heffte_gb300_plan plan, int variant, int tile_div, int radix_policy);
+/* Precision form of the plan's complex<float> 1-D passes: enable = 1 evaluates
+ * their radix-16 butterflies as 16-point DFT contractions on the tensor cores
+ * (tcgen05, operands split into three BF16 terms, FP32 accumulation; lengths
+ * 16^s * {1,2,4,8} in [64, 4096], other lengths keep the FP32 kernels);
+ * enable = 0 (default) is the plain FP32 form.  No counterpart in the
+ * reference, whose GPU backends call cuFFT / rocFFT / oneMKL
+ * (src/heffte_backend_cuda.cu). */
+int heffte_gb300_plan_set_tensor_cores(heffte_gb300_plan plan, int enable);
 /* The 18 features the selector reads for a transform of `kind` and `prec`. */
 int heffte_gb300_plan_features(int kind, int prec, const int size[3], float *features);
 /* Candidate c in [0, 16): use_reorder = c & 1, variant = (c >> 1) & 1,
