@@ -266,6 +266,8 @@ def ours(args, rank, world, local_rank):
     e2e_val = world * 2 * flops_per_transform(N) / (e2e_ms / 1e3) / 1e9
     rt_host = float(np.abs(hz.numpy() - hx.numpy()).max())
 
+    tc = tensor_core_form(gb, box, x, y, z, work, stream, args, ms_step, world) if prec == 0 else None
+
     if rank != 0:
         return
     cpu = None
@@ -300,8 +302,62 @@ def ours(args, rank, world, local_rank):
         "gpu_launches": 6 * args.steps,
         "clocks": clk,
         "accuracy": {"roundtrip_max_abs": rt_err, "roundtrip_max_abs_e2e": rt_host},
+        "tensor_cores": tc,
     }
     print(json.dumps(line), flush=True)
+
+
+def fp64_check(gb, box, x, stream, forms):
+    """rel-L2 of the forward transform of x by each plan in `forms` against this
+    library's complex<double> transform of the same input (the FP64 path the
+    parity tests hold to 1e-12 of the FP64 oracle)."""
+    import torch
+    p64 = gb.fft3d(box, box, stream=stream)
+    x64 = x.to(torch.complex128)
+    y64 = torch.empty_like(x64)
+    p64.forward(x64, y64)
+    del x64
+    out = {}
+    for name, p in forms.items():
+        y = torch.empty_like(x)
+        p.forward(x, y)
+        out[name] = float((torch.linalg.vector_norm(y.to(torch.complex128) - y64) / torch.linalg.vector_norm(y64)).item())
+        del y
+    return out
+
+
+def tensor_core_form(gb, box, x, y, z, work, stream, args, ms_fp32, world):
+    """The same workload with the radix-16 stages as split-BF16 DFT contractions
+    on the tensor cores (plan.set_tensor_cores), timed over the same steps."""
+    import torch
+    plan_tc = gb.fft3d(box, box, stream=stream)
+    plan_tc.set_tensor_cores(True)
+
+    def step():
+        plan_tc.forward_buffered(x, y, work, gb.scale.full)
+        plan_tc.backward_buffered(y, z, work, gb.scale.none)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    n_total = box.count()
+    plan_fp32 = gb.fft3d(box, box, stream=stream)
+    acc = fp64_check(gb, box, x, stream, {"fp32": plan_fp32, "tensor_cores": plan_tc})
+    step_bytes = 6 * 2.0 * n_total * 8
+    peak, _ = peaks()
+    return {"form": "radix-16 stages as 16-point DFT contractions on tcgen05, operands in three fixed-point "
+                    "BF16 slices, exact FP32 group sums in TMEM",
+            "value": world * 2 * flops_per_transform(n_total) / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
+            "ms_per_step": ms, "speedup_vs_fp32": ms_fp32 / ms,
+            "step_gbs": step_bytes / (ms / 1e3) / 1e9, "step_frac": step_bytes / (ms / 1e3) / 1e9 / peak,
+            "rel_l2_forward_vs_fp64": acc["tensor_cores"], "rel_l2_forward_vs_fp64_plain_fp32": acc["fp32"]}
 
 
 WORKLOADS = {
@@ -312,6 +368,11 @@ WORKLOADS = {
     "dct256": ("cos", (256, 256, 256), 0),
     "z2z512": ("c2c", (512, 512, 512), 1),
     "c2c1024x1024x512": ("c2c", (1024, 1024, 512), 0),
+    # the same two c2c float boxes with the radix-16 stages on the tensor cores
+    "c2c512tc": ("c2c", (512, 512, 512), 0, True),
+    "c2c1024x1024x512tc": ("c2c", (1024, 1024, 512), 0, True),
+    # small case (256 MiB, above L2) for ncu captures of the tensor-core kernel
+    "c2c512x512x128tc": ("c2c", (512, 512, 128), 0, True),
     "z2z64": ("c2c", (64, 64, 64), 1),
     # small case (256 MiB, above L2) for ncu captures of the c2c pass kernels
     "c2c512x512x128": ("c2c", (512, 512, 128), 0),
@@ -424,7 +485,8 @@ def algorithmic_bytes(kind, size, prec):
 def run_workload(name, steps, warmup):
     import torch
     import heffte_gb300 as gb
-    kind, size, prec = WORKLOADS[name]
+    kind, size, prec = WORKLOADS[name][:3]
+    tc = len(WORKLOADS[name]) > 3 and WORKLOADS[name][3]
     if kind == "batch":
         cache = "loop" if size == "loop" else None
         if size == "tuned":
@@ -440,6 +502,8 @@ def run_workload(name, steps, warmup):
     gen.manual_seed(99)
     if kind == "c2c":
         plan = gb.fft3d(box, box, stream=stream)
+        if tc:
+            plan.set_tensor_cores(True)
         x = torch.complex(torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1,
                           torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1)
         y, z = torch.empty_like(x), torch.empty_like(x)
@@ -474,8 +538,14 @@ def run_workload(name, steps, warmup):
     ms = e0.elapsed_time(e1) / steps
     b = 2 * algorithmic_bytes(kind, size, prec)
     peak, _ = peaks()
-    return {"workload": name, "ms_per_step": ms, "gflops": 2 * flops_per_transform(N) / (ms / 1e3) / 1e9,
-            "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak, "roundtrip_max_abs": err}
+    out = {"workload": name, "ms_per_step": ms, "gflops": 2 * flops_per_transform(N) / (ms / 1e3) / 1e9,
+           "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak, "roundtrip_max_abs": err}
+    if kind == "c2c" and prec == 0:
+        del y, z, work
+        out["rel_l2_forward_vs_fp64"] = fp64_check(gb, box, x, stream, {"p": plan})["p"]
+    if tc:
+        out["tensor_cores"] = True
+    return out
 
 
 def main():

@@ -129,6 +129,7 @@ class kind:
     r2c = 1
     cos = 2
     sin = 3
+    cos1 = 4
 
 
 class box3d:
@@ -304,9 +305,9 @@ def fft3d_r2c(inbox, outbox, r2c_direction, options=None, stream=None):
 
 
 def rtransform(rkind, inbox, outbox, options=None, stream=None):
-    """heffte::rtransform<backend::gb300_cos|gb300_sin> (include/heffte_fft3d.h:748-749)."""
-    if rkind not in (kind.cos, kind.sin):
-        raise heffte_input_error("rtransform kind must be kind.cos or kind.sin")
+    """heffte::rtransform<backend::gb300_cos|gb300_sin|gb300_cos1> (include/heffte_fft3d.h:748-749)."""
+    if rkind not in (kind.cos, kind.sin, kind.cos1):
+        raise heffte_input_error("rtransform kind must be kind.cos, kind.sin or kind.cos1")
     return _plan(rkind, inbox, outbox, 0, options, stream)
 
 

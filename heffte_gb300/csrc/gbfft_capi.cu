@@ -159,7 +159,7 @@ int heffte_gb300_executor_create(int kind, const long long low[3], const long lo
     return guard([&]{
         if (!out || !low || !high || !dims) throw Error(ST_INVALID, "null pointer");
         *out = nullptr;
-        if (kind < 0 || kind > 3) throw Error(ST_INVALID, "unknown executor kind");
+        if (kind < 0 || kind > 4) throw Error(ST_INVALID, "unknown executor kind");
         if (ndims < 1 || ndims > 3) throw Error(ST_INVALID, "ndims must be 1, 2 or 3");
         Box3 box({low[0], low[1], low[2]}, {high[0], high[1], high[2]}, order_of(order));
         std::vector<int> d(dims, dims + ndims);
@@ -220,7 +220,7 @@ int heffte_gb300_plan_create(int kind, const int inbox_low[3], const int inbox_h
         if (!plan) throw Error(ST_INVALID, "null plan pointer");
         *plan = nullptr;
         if (!inbox_low || !inbox_high || !outbox_low || !outbox_high) throw Error(ST_INVALID, "null box pointer");
-        if (kind < 0 || kind > 3) throw Error(ST_INVALID, "unknown transform kind");
+        if (kind < 0 || kind > 4) throw Error(ST_INVALID, "unknown transform kind");
         Box3 ib({inbox_low[0], inbox_low[1], inbox_low[2]}, {inbox_high[0], inbox_high[1], inbox_high[2]},
                 order_of(inbox_order));
         Box3 ob({outbox_low[0], outbox_low[1], outbox_low[2]}, {outbox_high[0], outbox_high[1], outbox_high[2]},

@@ -380,6 +380,21 @@ void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void c
     run(s, K_C2R, prec, cols, a);
 }
 
+void launch_dct1(cudaStream_t s, Fft1D &f, int prec, bool fwd, int N, Layout Li, Layout Lo, void const *in, void *out,
+                 long long G, double scale, LaunchCfg cfg){
+    if (G <= 0) return;
+    if (N < 2 || f.N != 2 * (N - 1)) throw Error(ST_INVALID, "DCT-I of N values runs on an FFT of length 2(N-1)");
+    KernelArgs a{};
+    bool cols = is_cols(Li, Lo);
+    geometry(f, prec, cols, true, G, cfg, a);
+    a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
+    a.tw = f.twiddles(prec, s);
+    double sc = fwd ? scale : 2.0 * scale;
+    a.scale = sc; a.do_scale = (sc != 1.0);
+    a.ndata = N;
+    run(s, K_DCT1, prec, cols, a);
+}
+
 void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout Li, Layout Lo, void const *in,
                 void *out, long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;

@@ -79,6 +79,9 @@ void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void c
                 long long G, double scale, LaunchCfg cfg = {});
 void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg = {});
+// DCT-I (REDFT00, backward 2 x REDFT00) of lines of N values; f has length 2(N-1).
+void launch_dct1(cudaStream_t s, Fft1D &f, int prec, bool fwd, int N, Layout Li, Layout Lo, void const *in, void *out,
+                 long long G, double scale, LaunchCfg cfg = {});
 void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout Li, Layout Lo, void const *in,
                 void *out, long long G, double scale, LaunchCfg cfg = {});
 
@@ -108,8 +111,9 @@ struct KernelArgs {
     double scale;
     int do_scale;
     int sine;
+    int ndata;          // line length of the DCT-I kernel (the FFT has length 2(ndata - 1))
 };
-enum Kind { K_C2C_F, K_C2C_B, K_R2C, K_C2R, K_R2R_F, K_R2R_B };
+enum Kind { K_C2C_F, K_C2C_B, K_R2C, K_C2R, K_R2R_F, K_R2R_B, K_DCT1 };
 void launch_kernel_f32(cudaStream_t s, int kind, bool cols, KernelArgs const &a);
 void launch_kernel_f64(cudaStream_t s, int kind, bool cols, KernelArgs const &a);
 

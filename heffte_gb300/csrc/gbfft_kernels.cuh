@@ -330,4 +330,42 @@ k_r2r(Plan1D P, Layout Li, Layout Lo, T const *in, T *out, c_t<T> const *__restr
     }
 }
 
+// ---------------------------------------------------------------------------
+// DCT-I (REDFT00) of lines of N >= 2 values, the reference's cos1 transform:
+//   y_k = x_0 + (-1)^k x_{N-1} + 2 sum_{n=1}^{N-2} x_n cos(pi n k / (N-1)),
+// forward = REDFT00, backward = 2 x REDFT00.  The DFT of the even extension
+//   e = (x_0, x_1, ..., x_{N-1}, x_{N-2}, ..., x_1)   (length L = 2(N-1))
+// is real and equals REDFT00 on k < N, so two lines share one complex FFT of
+// length L: z = e_a + i e_b, y_a = Re Z, y_b = Im Z.  P is the plan of length L.
+// ---------------------------------------------------------------------------
+template<typename T, int EMAX, bool COLS>
+__global__ void __launch_bounds__(512)
+k_dct1(Plan1D P, int N, Layout Li, Layout Lo, T const *in, T *out, c_t<T> const *__restrict__ tw,
+       long long G, int TPB, T scale, int do_scale){
+    using C = c_t<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C*>(smraw);
+    int loc, t;
+    thread_map<COLS>(TPB, P.T, loc, t);
+    long long gp = (long long)blockIdx.x * TPB + loc;
+    long long ga = 2 * gp, gb = 2 * gp + 1;
+    bool active = (ga < G) && (t < P.T) && (loc < TPB);
+    bool hasb = gb < G;
+    long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
+    long long oa = active ? base_of(Lo, ga) : 0, obb = (active && hasb) ? base_of(Lo, gb) : 0;
+    long long ies = Li.estride, oes = Lo.estride;
+    int const L = P.N;
+    T s = do_scale ? scale : (T)1;
+    auto ld = [&](int p) -> C {
+        int n = (p < N) ? p : L - p;
+        C z; z.x = in[ia + n * ies]; z.y = hasb ? in[ibb + n * ies] : (T)0; return z;
+    };
+    auto st = [&](int k, C v){
+        if (k >= N) return;
+        out[oa + k * oes] = v.x * s;
+        if (hasb) out[obb + k * oes] = v.y * s;
+    };
+    fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padded_len(L), tw, true, ld, st);
+}
+
 } // namespace gbfft

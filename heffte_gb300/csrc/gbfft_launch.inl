@@ -63,6 +63,12 @@ void dispatch(cudaStream_t s, int kind, KernelArgs const &a){
                                           a.G, a.tpb, a.sine, sc, a.do_scale);
             break;
         }
+        case K_DCT1: {
+            auto k = k_dct1<T, kEmax, COLS>; prepare<k_dct1<T, kEmax, COLS>>();
+            k<<<grid, block, a.smem, s>>>(*a.plan, a.ndata, a.Li, a.Lo, (T const*)a.in, (T*)a.out, (C const*)a.tw,
+                                          a.G, a.tpb, sc, a.do_scale);
+            break;
+        }
         default: throw Error(ST_INVALID, "unknown kernel kind");
     }
     check_cuda(cudaPeekAtLastError(), "fft kernel launch");

@@ -178,7 +178,7 @@ void plan_features(int kind, int prec, int const size[3], float *f){
     f[k++] = (float)(std::log2(total) / 30.0);
     f[k++] = (kind == PK_C2C) ? 1.f : 0.f;
     f[k++] = (kind == PK_R2C) ? 1.f : 0.f;
-    f[k++] = (kind == PK_COS || kind == PK_SIN) ? 1.f : 0.f;
+    f[k++] = (kind == PK_COS || kind == PK_SIN || kind == PK_COS1) ? 1.f : 0.f;
     f[k++] = (float)prec;
     for (int d = 0; d < 3; d++){
         int n = size[d];

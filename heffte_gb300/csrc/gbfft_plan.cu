@@ -52,9 +52,17 @@ std::unique_ptr<Executor> make_executor(int kind, Box3 const &box, std::vector<i
     e->dims = dims;
     for (int d : dims){
         if (d < 0 || d > 2) throw Error(ST_INVALID, "invalid dimension");
-        if (!supported_length((int)box.size[d], 1))
+        int n = (int)box.size[d];
+        if (kind == EX_COS1){
+            // DCT-I of n values runs on an FFT of length 2(n - 1)
+            if (n < 2 || !supported_length(2 * (n - 1), 1))
+                throw Error(ST_UNSUPPORTED, "DCT-I length " + std::to_string(n) + " is not supported (needs n >= 2 and 2(n-1) supported)");
+            e->ffts.push_back(get_fft1d(2 * (n - 1)));
+            continue;
+        }
+        if (!supported_length(n, 1))
             throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(box.size[d]) + " is not supported");
-        e->ffts.push_back(get_fft1d((int)box.size[d]));
+        e->ffts.push_back(get_fft1d(n));
     }
     return e;
 }
@@ -71,6 +79,7 @@ void Executor::forward(cudaStream_t s, int prec, void const *in, void *out, doub
         double sc = (i + 1 == dims.size()) ? scale : 1.0;
         Layout L = pass_layout(box, dims[i], box.order);
         if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, true, L, L, src, out, batch_count(box, dims[i]), sc);
+        else if (kind == EX_COS1) launch_dct1(s, *ffts[i], prec, true, (int)box.size[dims[i]], L, L, src, out, batch_count(box, dims[i]), sc);
         else launch_r2r(s, *ffts[i], prec, true, kind == EX_SIN, L, L, src, out, batch_count(box, dims[i]), sc);
         src = out;
     }
@@ -88,6 +97,7 @@ void Executor::backward(cudaStream_t s, int prec, void const *in, void *out, dou
         double sc = (i + 1 == dims.size()) ? scale : 1.0;
         Layout L = pass_layout(box, dims[i], box.order);
         if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, false, L, L, src, out, batch_count(box, dims[i]), sc);
+        else if (kind == EX_COS1) launch_dct1(s, *ffts[i], prec, false, (int)box.size[dims[i]], L, L, src, out, batch_count(box, dims[i]), sc);
         else launch_r2r(s, *ffts[i], prec, false, kind == EX_SIN, L, L, src, out, batch_count(box, dims[i]), sc);
         src = out;
     }
@@ -128,7 +138,7 @@ std::array<int, 3> order_with_first(std::array<int, 3> const &cur, int d){
 //   out_holds_inter: the output buffer has the element type of the intermediate data
 std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_box, Box3 const &dst_box,
                           Box3 const &inter_geom, bool reorder, bool out_holds_inter, bool in_aliases_out,
-                          int &work_buffers, int radix_policy){
+                          int &work_buffers, int radix_policy, bool dct1 = false){
     // drop length-1 complex passes (identity), keep at least one op to move
     // the data; a length-1 r2r transform is not the identity (REDFT10 of one
     // value is twice the value) and r2c/c2r change the element type
@@ -163,8 +173,8 @@ std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_b
         }
         f.dbox = next;
         f.ref_order = cur.order;
-        f.fft = fft_for((int)((p.kind == K_R2C) ? cur.size[p.dim] : (p.kind == K_C2R ? dst_box.size[p.dim] : cur.size[p.dim])),
-                        radix_policy);
+        int n = (int)((p.kind == K_R2C) ? cur.size[p.dim] : (p.kind == K_C2R ? dst_box.size[p.dim] : cur.size[p.dim]));
+        f.fft = fft_for(dct1 ? 2 * (n - 1) : n, radix_policy);
         ops.push_back(f);
         cur = next;
     }
@@ -250,6 +260,12 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
     p->outbox = outbox;
     for (int d = 0; d < 3; d++){
         int n = (int)inbox.size[d];
+        if (kind == PK_COS1){
+            if (n < 2 || !supported_length(2 * (n - 1), 1))
+                throw Error(ST_UNSUPPORTED, "DCT-I length " + std::to_string(n) + " is not supported (needs n >= 2 and "
+                            "2(n-1) with prime factors 2, 3, 5, 7, 11, 13 up to " + std::to_string(max_length(1)) + ")");
+            continue;
+        }
         if (!supported_length(n, 1))
             throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(n) +
                         " is not supported (lengths up to " + std::to_string(max_length(1)) +
@@ -258,17 +274,20 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
     std::array<int, 3> io = inbox.order, oo = outbox.order;
     bool reorder = o.use_reorder;
     int wf = 0, wb = 0, wfa = 0;
-    if (kind == PK_C2C || kind == PK_COS || kind == PK_SIN){
+    if (kind == PK_C2C || kind == PK_COS || kind == PK_SIN || kind == PK_COS1){
         bool r2r = (kind != PK_C2C);
+        bool dct1 = (kind == PK_COS1);
         std::vector<PassSpec> fwd, bwd;
         for (int i = 0; i < 3; i++) fwd.push_back({r2r ? K_R2R_F : K_C2C_F, io[i]});
         for (int i = 0; i < 3; i++) bwd.push_back({r2r ? K_R2R_B : K_C2C_B, oo[i]});
-        p->fwd = build_ops(fwd, inbox, outbox, inbox, reorder, true, false, wf, knobs.radix_policy);
+        p->fwd = build_ops(fwd, inbox, outbox, inbox, reorder, true, false, wf, knobs.radix_policy, dct1);
         p->fwd_alias = p->fwd;
-        p->bwd = build_ops(bwd, outbox, inbox, inbox, reorder, true, false, wb, knobs.radix_policy);
+        p->bwd = build_ops(bwd, outbox, inbox, inbox, reorder, true, false, wb, knobs.radix_policy, dct1);
         p->work_elems = std::max(wf, wb) * inbox.count();
         double n = (double)inbox.count();
-        p->scale_factor = r2r ? 1.0 / (64.0 * n) : 1.0 / n;
+        // include/heffte_fft3d.h:635-650: 1/(64 N) for the cos/sin tags, 1/(64 prod(n_i - 1)) for DCT-I
+        double n1 = (double)(inbox.size[0] - 1) * (double)(inbox.size[1] - 1) * (double)(inbox.size[2] - 1);
+        p->scale_factor = dct1 ? 1.0 / (64.0 * n1) : (r2r ? 1.0 / (64.0 * n) : 1.0 / n);
     } else {
         Box3 cgeom = inbox.r2c(r2c_dir);
         std::vector<PassSpec> fwd{{K_R2C, r2c_dir}}, bwd;
@@ -294,7 +313,7 @@ double Plan3D::get_scale(int scaling) const{
 }
 
 static int elem_dtype(int kind, int prec, bool complex_side){
-    if (kind == PK_COS || kind == PK_SIN) return prec == 0 ? DT_FLOAT : DT_DOUBLE;
+    if (kind == PK_COS || kind == PK_SIN || kind == PK_COS1) return prec == 0 ? DT_FLOAT : DT_DOUBLE;
     if (complex_side) return prec == 0 ? DT_CFLOAT : DT_CDOUBLE;
     return prec == 0 ? DT_FLOAT : DT_DOUBLE;
 }
@@ -353,8 +372,15 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
                     case K_C2C_B: launch_c2c(stream, *op.fft, prec, false, Li, Lo, src, dst, G, s, cfg); break;
                     case K_R2C: launch_r2c(stream, *op.fft, prec, Li, Lo, src, dst, G, s, cfg); break;
                     case K_C2R: launch_c2r(stream, *op.fft, prec, Li, Lo, src, dst, G, s, cfg); break;
-                    case K_R2R_F: launch_r2r(stream, *op.fft, prec, true, kind == PK_SIN, Li, Lo, src, dst, G, s, cfg); break;
-                    case K_R2R_B: launch_r2r(stream, *op.fft, prec, false, kind == PK_SIN, Li, Lo, src, dst, G, s, cfg); break;
+                    case K_R2R_F:
+                    case K_R2R_B: {
+                        bool f = (op.kind == K_R2R_F);
+                        if (kind == PK_COS1)
+                            launch_dct1(stream, *op.fft, prec, f, (int)op.sbox.size[op.dim], Li, Lo, src, dst, G, s, cfg);
+                        else
+                            launch_r2r(stream, *op.fft, prec, f, kind == PK_SIN, Li, Lo, src, dst, G, s, cfg);
+                        break;
+                    }
                 }
             } else if (op.type == Op::RESHAPE){
                 Box3 const &A = op.sbox, &B = op.dbox;

@@ -42,7 +42,7 @@ bool valid_order(std::array<int, 3> const &o);
 // varies fastest in g).
 Layout pass_layout(Box3 const &box, int dim, std::array<int, 3> const &ref_order);
 
-enum ExecKind { EX_C2C = 0, EX_R2C = 1, EX_COS = 2, EX_SIN = 3 };
+enum ExecKind { EX_C2C = 0, EX_R2C = 1, EX_COS = 2, EX_SIN = 3, EX_COS1 = 4 };
 
 // One executor: the role of cufft_executor / cufft_executor_r2c /
 // real2real_executor (include/heffte_backend_cuda.h:436-751,
@@ -69,7 +69,7 @@ struct Options {
     bool use_gpu_aware = true;
 };
 
-enum PlanKind { PK_C2C = 0, PK_R2C = 1, PK_COS = 2, PK_SIN = 3 };
+enum PlanKind { PK_C2C = 0, PK_R2C = 1, PK_COS = 2, PK_SIN = 3, PK_COS1 = 4 };
 
 // Tuning knobs of a plan (the choices the learned selector makes): kernel
 // family (0 pipelined where it applies, 1 generic only), tile of the generic

@@ -26,7 +26,7 @@
 //     96 BF16 per MMA batch, [a0 | a1 | a2] x 32 reals) in the K-major
 //     no-swizzle core-matrix layout;
 //   * B is the real 32x32 form of the 16-point DFT matrix (three 32x32 BF16
-//     slices, built once per CTA from exact sincospi values);
+//     slices, built once per direction on the host and copied in by each CTA);
 //   * one thread issues the six slice products (two K=16 steps each) into
 //     three 128x32 FP32 accumulators in TMEM and commits them to an mbarrier;
 //   * each warp reads its 32 TMEM lanes back (tcgen05.ld 32x32b), combines the
@@ -43,6 +43,10 @@
 #include "gbfft_internal.h"
 #include <cuda_bf16.h>
 #include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
 
 namespace gbfft {
 
@@ -153,7 +157,7 @@ template<int N> struct TcShape {
     static constexpr int S16 = (N >= 4096) ? 3 : (N >= 256) ? 2 : 1;
     static constexpr int R0 = N / ((S16 == 3) ? 4096 : (S16 == 2) ? 256 : 16);
     static constexpr int DATA_BYTES = LT * PADN * 8;
-    static constexpr int SMEM = kBbytes + kBatches * kAbytes + ((DATA_BYTES + 15) / 16) * 16 + 16;
+    static constexpr int SMEM = kBbytes + kBatches * kAbytes + ((DATA_BYTES + 15) / 16) * 16 + 8 * kBatches + 16;
     static_assert(R0 == 1 || R0 == 2 || R0 == 4 || R0 == 8, "length must be 16^s * {1, 2, 4, 8}");
     static_assert(LT >= 1 && LT * N == kTile, "length must divide the tile");
 };
@@ -172,6 +176,7 @@ struct TcArgs {
     float2 const *in;
     float2 *out;
     float2 const *tw;
+    uint4 const *bmat;         // B operand image (kBbytes), built once per direction and device
     long long G, ntiles;
     float scale;
     int do_scale;
@@ -199,32 +204,17 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
     unsigned char *As = smem + kBbytes;
     float2 *D = reinterpret_cast<float2*>(smem + kBbytes + kBatches * kAbytes);
     uint64_t *bar = reinterpret_cast<uint64_t*>(smem + kBbytes + kBatches * kAbytes + ((Sh::DATA_BYTES + 15) / 16) * 16);
-    uint32_t *slot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint32_t *slot = reinterpret_cast<uint32_t*>(bar + kBatches);
     int const tid = threadIdx.x, warp = tid >> 5;
 
     if (warp == 0){ tmem_alloc(slot, kTmemCols); tmem_relinquish(); }
-    // B: real 32x32 form of the 16-point DFT, rows n = output (2m + re/im),
-    // columns k = input (2k' + re/im), three integer BF16 slices, K-major core matrices
-    for (int e = tid; e < 32 * 32; e += kThreads){
-        int n = e >> 5, k = e & 31;
-        int m = n >> 1, kk = k >> 1, ro = n & 1, ri = k & 1;
-        double s, c;
-        sincospi((double)((m * kk) & 15) / 8.0, &s, &c);
-        double v;
-        if (FWD) v = ro == 0 ? (ri == 0 ? c : s) : (ri == 0 ? -s : c);        // exp(-i t)
-        else     v = ro == 0 ? (ri == 0 ? c : -s) : (ri == 0 ? s : c);        // exp(+i t)
-        double t = v * 256.0, b0 = rint(t);
-        double r = (t - b0) * 512.0, b1 = rint(r);
-        double b2 = rint((r - b1) * 512.0);
-        __nv_bfloat16 h = __float2bfloat16_rn((float)b0);
-        __nv_bfloat16 md = __float2bfloat16_rn((float)b1);
-        __nv_bfloat16 lo = __float2bfloat16_rn((float)b2);
-        int off = (k >> 3) * 512 + (n >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
-        *reinterpret_cast<__nv_bfloat16*>(Bs + 0 * 2048 + off) = h;
-        *reinterpret_cast<__nv_bfloat16*>(Bs + 1 * 2048 + off) = md;
-        *reinterpret_cast<__nv_bfloat16*>(Bs + 2 * 2048 + off) = lo;
+    // B operand: the three DFT slices, already in the shared-memory layout
+    for (int i = tid; i < kBbytes / 16; i += kThreads)
+        reinterpret_cast<uint4*>(Bs)[i] = __ldg(a.bmat + i);
+    if (tid == 0){
+        for (int bb = 0; bb < kBatches; bb++) mbar_init(&bar[bb], 1);
+        fence_mbar_init();
     }
-    if (tid == 0){ mbar_init(bar, 1); fence_mbar_init(); }
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -237,37 +227,49 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
     uint32_t phase = 0;
     bool fail = false;
     int rexp[kBatches];
+    // The raw values of a tile, kPer per thread, are loaded into registers one
+    // tile ahead: the loads of tile t+1 are in flight while the tensor-core
+    // stages of tile t run.  Value i of a thread is element e = tid + 128 i of
+    // the tile (r0 = 1), or input q of butterfly b = tid + 128 (i / r0) of
+    // the leading radix-r0 stage (i % r0 = q).
+    constexpr int kPer = kTile / kThreads;
+    constexpr int NRr = N / R0;
+    float2 pre[kPer];
+    auto issue_loads = [&](long long tile){
+        long long const g0 = tile * LT;
+        #pragma unroll
+        for (int i = 0; i < kPer / R0; i++){
+            int b = tid + kThreads * i;
+            int l, p0, step;
+            if constexpr (R0 == 1){ l = COLS ? b % LT : b / N; p0 = COLS ? b / LT : b % N; step = 0; }
+            else { l = COLS ? b % LT : b / NRr; p0 = COLS ? b / LT : b % NRr; step = NRr; }
+            long long g = g0 + l;
+            bool ok = g < a.G;
+            long long base = ok ? base_of(a.Li, g) : 0;
+            #pragma unroll
+            for (int q = 0; q < R0; q++)
+                pre[i * R0 + q] = ok ? __ldcs(a.in + base + (long long)(p0 + q * step) * a.Li.estride) : make_float2(0.f, 0.f);
+        }
+    };
+    if ((long long)blockIdx.x < a.ntiles) issue_loads(blockIdx.x);
     for (long long tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x){
         long long const g0 = tile * LT;
-        // ---- load the tile (fused with the leading radix-r0 stage)
-        if constexpr (R0 == 1){
-            for (int e = tid; e < kTile; e += kThreads){
-                int l = COLS ? e % LT : e / N, p = COLS ? e / LT : e % N;
-                long long g = g0 + l;
-                float2 v = make_float2(0.f, 0.f);
-                if (g < a.G) v = a.in[base_of(a.Li, g) + (long long)p * a.Li.estride];
-                D[sidx(PADN, l, p)] = v;
-            }
-        } else {
-            constexpr int NRr = N / R0;
-            for (int b = tid; b < LT * NRr; b += kThreads){
+        // ---- the tile into shared memory (through the leading radix-r0 stage)
+        #pragma unroll
+        for (int i = 0; i < kPer / R0; i++){
+            int b = tid + kThreads * i;
+            if constexpr (R0 == 1){
+                int l = COLS ? b % LT : b / N, p = COLS ? b / LT : b % N;
+                D[sidx(PADN, l, p)] = pre[i];
+            } else {
                 int l = COLS ? b % LT : b / NRr, j = COLS ? b / LT : b % NRr;
-                long long g = g0 + l;
-                float2 v[R0];
-                if (g < a.G){
-                    long long base = base_of(a.Li, g);
-                    #pragma unroll
-                    for (int q = 0; q < R0; q++) v[q] = a.in[base + (long long)(j + q * NRr) * a.Li.estride];
-                } else {
-                    #pragma unroll
-                    for (int q = 0; q < R0; q++) v[q] = make_float2(0.f, 0.f);
-                }
-                bfly<R0, FWD, float2, float>(v);
+                bfly<R0, FWD, float2, float>(&pre[i * R0]);
                 #pragma unroll
-                for (int q = 0; q < R0; q++) D[sidx(PADN, l, j * R0 + q)] = v[q];
+                for (int q = 0; q < R0; q++) D[sidx(PADN, l, j * R0 + q)] = pre[i * R0 + q];
             }
         }
         __syncthreads();
+        if (tile + gridDim.x < a.ntiles) issue_loads(tile + gridDim.x);
         // ---- radix-16 stages on the tensor cores
         for (int s = first16; s < P.nstages; s++){
             Stage const S = P.st[s];
@@ -305,14 +307,12 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                     st_shared_v4(rowaddr + (4 + c) * kChunk, m[0], m[1], m[2], m[3]);
                     st_shared_v4(rowaddr + (8 + c) * kChunk, lo[0], lo[1], lo[2], lo[3]);
                 }
-            }
-            fence_proxy_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            if (tid == 0){
-                tc_fence_after();
-                #pragma unroll
-                for (int bb = 0; bb < kBatches; bb++){
+                // this batch's MMAs run while the next batch is built
+                fence_proxy_async_smem();
+                tc_fence_before();
+                __syncthreads();
+                if (tid == 0){
+                    tc_fence_after();
                     #pragma unroll
                     for (int pr = 0; pr < 6; pr++){
                         #pragma unroll
@@ -323,16 +323,17 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                                      !(group_first(pr) && ks == 0));
                         }
                     }
+                    mma_commit(&bar[bb]);
                 }
-                mma_commit(bar);
+                __syncwarp();
             }
-            bool ok = mma_wait(bar, phase, a.status);
-            phase ^= 1;
-            if (__syncthreads_or(!ok)){ fail = true; break; }
-            tc_fence_after();
-            // D rows back from TMEM
+            // D rows back from TMEM, batch by batch (every gather of the stage
+            // is done, so the tile can be overwritten)
+            bool ok = true;
             #pragma unroll
             for (int bb = 0; bb < kBatches; bb++){
+                ok = mma_wait(&bar[bb], phase, a.status) && ok;
+                tc_fence_after();
                 uint32_t const taddr = tbase + ((uint32_t)(warp * 32) << 16) + bb * kBatchCols;
                 float y[32];
                 {
@@ -370,14 +371,15 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                         D[sidx(PADN, l, ob + q * S.Ns)] = make_float2(y[2 * q], y[2 * q + 1]);
                 }
             }
+            phase ^= 1;
             tc_fence_before();
-            __syncthreads();
+            if (__syncthreads_or(!ok)){ fail = true; break; }
         }
         if (fail) break;
     }
     if (fail){
         // one more bounded wait for the MMAs in flight before the memory is freed
-        mma_wait(bar, phase ^ 1, nullptr);
+        for (int bb = 0; bb < kBatches; bb++) mma_wait(&bar[bb], phase ^ 1, nullptr);
     }
     __syncthreads();
     if (warp == 0){
@@ -393,11 +395,21 @@ void launch_kernel(cudaStream_t s, TcArgs const &a){
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
     if (!(done_mask & (1 << dev))){
         check_cuda(cudaFuncSetAttribute(Kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM), "smem attribute");
+        // the whole unified L1 / shared array as shared memory: two CTAs per SM
+        check_cuda(cudaFuncSetAttribute(Kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100), "carveout attribute");
         done_mask |= 1 << dev;
     }
-    int per_sm = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kfn, kThreads, SMEM), "occupancy");
-    // tensor memory: every resident CTA holds kTmemCols of the SM's 512 columns
+    // resident CTAs per SM from the device's limits: shared memory (with the
+    // per-block reservation), registers, and tensor memory (every resident
+    // CTA holds kTmemCols of the SM's 512 columns)
+    int smem_sm = 0, smem_rsv = 0, regs_sm = 0;
+    check_cuda(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev), "device attribute");
+    check_cuda(cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev), "device attribute");
+    check_cuda(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev), "device attribute");
+    cudaFuncAttributes fa{};
+    check_cuda(cudaFuncGetAttributes(&fa, Kfn), "function attributes");
+    int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * (kThreads / 32);
+    int per_sm = std::min(smem_sm / (SMEM + smem_rsv), regs_sm / std::max(regs_cta, 1));
     per_sm = std::max(1, std::min(per_sm, (int)(512 / kTmemCols)));
     long long grid = std::min<long long>(a.ntiles, (long long)per_sm * num_sms());
     Kfn<<<(unsigned)grid, kThreads, SMEM, s>>>(a);
@@ -414,6 +426,55 @@ void launch_n(cudaStream_t s, bool fwd, bool cols, TcArgs const &a){
         if (cols) launch_kernel<k_tc_c2c<N, false, true>, SM>(s, a);
         else      launch_kernel<k_tc_c2c<N, false, false>, SM>(s, a);
     }
+}
+
+// The B operand of one direction: rows n = output (2m + re/im), columns
+// k = input (2k' + re/im) of the real 32x32 form of the 16-point DFT, each
+// entry w = 2^-8 (b0 + b1/512 + b2/512^2) (integers |b| <= 256, exact in
+// BF16), three slices of 2048 bytes in the K-major core-matrix layout
+// (K chunks of 8 at 512 bytes, row groups of 8 at 128 bytes).
+std::vector<uint16_t> dft16_slices(bool fwd){
+    std::vector<uint16_t> img(kBbytes / 2, 0);
+    double const pi = 3.14159265358979323846;
+    for (int n = 0; n < 32; n++){
+        for (int k = 0; k < 32; k++){
+            int m = n >> 1, kk = k >> 1, ro = n & 1, ri = k & 1;
+            double t = pi * (double)((m * kk) & 15) / 8.0;
+            double c = std::cos(t), s = std::sin(t);
+            double v;
+            if (fwd) v = ro == 0 ? (ri == 0 ? c : s) : (ri == 0 ? -s : c);     // exp(-i t)
+            else     v = ro == 0 ? (ri == 0 ? c : -s) : (ri == 0 ? s : c);     // exp(+i t)
+            double x = v * 256.0, b0 = std::nearbyint(x);
+            double r = (x - b0) * 512.0, b1 = std::nearbyint(r);
+            double b2 = std::nearbyint((r - b1) * 512.0);
+            int off = ((k >> 3) * 512 + (n >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2) / 2;
+            double b[3] = {b0, b1, b2};
+            for (int u = 0; u < 3; u++){
+                float f = (float)b[u];             // an integer of at most 9 bits: exact in BF16
+                uint32_t bits;
+                std::memcpy(&bits, &f, 4);
+                img[u * 1024 + off] = (uint16_t)(bits >> 16);
+            }
+        }
+    }
+    return img;
+}
+
+uint4 const *dft16_device(bool fwd){
+    static std::mutex mu;
+    static std::map<int, uint4*> tables[2];
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    auto &t = tables[fwd ? 0 : 1];
+    auto it = t.find(dev);
+    if (it != t.end()) return it->second;
+    std::vector<uint16_t> img = dft16_slices(fwd);
+    uint4 *d = nullptr;
+    check_cuda(cudaMalloc(&d, kBbytes), "cudaMalloc(DFT slices)");
+    check_cuda(cudaMemcpy(d, img.data(), kBbytes, cudaMemcpyHostToDevice), "copy DFT slices");
+    t[dev] = d;
+    return d;
 }
 
 } // namespace
@@ -445,6 +506,7 @@ void launch_tc_c2c(cudaStream_t s, int N, bool fwd, Layout Li, Layout Lo, void c
     a.in = static_cast<float2 const*>(in);
     a.out = static_cast<float2*>(out);
     a.tw = static_cast<float2 const*>(f->twiddles(0, s));
+    a.bmat = dft16_device(fwd);
     a.G = G;
     int lt = kTile / N;
     a.ntiles = (G + lt - 1) / lt;

@@ -49,11 +49,13 @@ extern "C" {
 #define HEFFTE_GB300_SCALE_SYMMETRIC 2
 
 /* transform kinds: fft3d (c2c), fft3d_r2c, rtransform<cos> (DCT-II / 2xDCT-III),
- * rtransform<sin> (DST-II / 2xDST-III) */
+ * rtransform<sin> (DST-II / 2xDST-III), rtransform<cos1> (DCT-I / 2xDCT-I,
+ * scale 1/(64 prod(n_i - 1)), every n_i >= 2) */
 #define HEFFTE_GB300_C2C 0
 #define HEFFTE_GB300_R2C 1
 #define HEFFTE_GB300_COS 2
 #define HEFFTE_GB300_SIN 3
+#define HEFFTE_GB300_COS1 4
 
 /* Message of the last failure on this thread ("" after a success). */
 const char *heffte_gb300_last_error(void);
@@ -148,9 +150,9 @@ typedef struct heffte_gb300_executor_s *heffte_gb300_executor;
  *   kind C2C: ndims = 1, 2 or 3 transform dimensions, the roles of the
  *             cufft_executor constructors (include/heffte_backend_cuda.h:445-491);
  *   kind R2C: ndims = 1, cufft_executor_r2c (:631-646);
- *   kind COS / SIN: ndims = 1, real2real_executor<cufft_cos|cufft_sin>
- *             (include/heffte_r2r_executor.h:191-210); unlike the reference
- *             the dimension need not be the fastest one.
+ *   kind COS / SIN / COS1: ndims = 1, real2real_executor<cufft_cos|cufft_sin|
+ *             cufft_cos1> (include/heffte_r2r_executor.h:191-210); unlike the
+ *             reference the dimension need not be the fastest one.
  * An empty box gives *out = NULL and HEFFTE_GB300_SUCCESS, as make_executor
  * returns a null pointer for empty boxes (include/heffte_common.h:669-676). */
 int heffte_gb300_executor_create(int kind, const long long low[3], const long long high[3], const int order[3],
@@ -193,7 +195,7 @@ int heffte_gb300_set_default_options(heffte_gb300_plan_options *options);
 /* heffte_plan_create / heffte_plan_create_r2c (include/heffte_c.h:78-105) for
  * one rank: the boxes span the whole index set; *_order may be NULL for
  * (0,1,2).  kind: HEFFTE_GB300_C2C, _R2C (outbox = inbox.r2c(r2c_direction)),
- * _COS or _SIN.  stream: the cudaStream_t every call of this plan uses
+ * _COS, _SIN or _COS1.  stream: the cudaStream_t every call of this plan uses
  * (NULL = default stream, a non-owning handle as in fft3d's constructor). */
 int heffte_gb300_plan_create(int kind, const int inbox_low[3], const int inbox_high[3], const int *inbox_order,
                              const int outbox_low[3], const int outbox_high[3], const int *outbox_order,

@@ -176,7 +176,7 @@ def test_known_answers_3d(gb, golden):
     x = ka["input"]
     y = run_c2c(gb, x.astype(np.complex128), (2, 3, 4), (0, 1, 2), (0, 1, 2), 0, 0, 1)
     assert np.allclose(y, ka["c2c_fwd"], atol=1e-11)
-    for kind, name in ((gb.kind.cos, "cos"), (gb.kind.sin, "sin")):
+    for kind, name in ((gb.kind.cos, "cos"), (gb.kind.sin, "sin"), (gb.kind.cos1, "cos1")):
         p = gb.rtransform(kind, gb.box3d((0, 0, 0), (1, 2, 3)), gb.box3d((0, 0, 0), (1, 2, 3)))
         t = dev(x)
         o = torch.empty_like(t)
@@ -209,10 +209,8 @@ def test_seeded_against_reference(gb, golden, reorder):
             want_f = O.fft3d_r2c(x, size, rd, io, oo)
         else:
             k = int(m["r2r_kind"])
-            if k == 2:
-                continue  # DCT-I is a later row
             ob = gb.box3d((0, 0, 0), [s - 1 for s in size], oo)
-            p = gb.rtransform(gb.kind.cos if k == 0 else gb.kind.sin, ib, ob, opts)
+            p = gb.rtransform((gb.kind.cos, gb.kind.sin, gb.kind.cos1)[k], ib, ob, opts)
             want_f = O.rtransform(k, x, size, io, oo)
         xin = dev(x)
         y = torch.empty(p.size_outbox(), dtype=torch.from_numpy(fwd_ref[:1]).dtype, device="cuda")
@@ -271,14 +269,29 @@ def test_r2c_sizes_against_fp64(gb, size, prec):
                 assert np.array_equal(host(y), yh), "c2r modified its input"
 
 
-@pytest.mark.parametrize("size", [(8, 8, 8), (7, 6, 5), (16, 9, 4), (1, 5, 3), (32, 24, 20)])
+def _smooth13(n):
+    for q in (2, 3, 5, 7, 11, 13):
+        while n % q == 0:
+            n //= q
+    return n == 1
+
+
+@pytest.mark.parametrize("size", [(8, 8, 8), (7, 6, 5), (16, 9, 4), (1, 5, 3), (32, 24, 20), (33, 25, 17),
+                                  (65, 9, 2), (257, 129, 65)])
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("rkind", [2, 3])
+@pytest.mark.parametrize("rkind", [2, 3, 4])
 def test_r2r_sizes_against_fp64(gb, size, prec, rkind):
+    # DCT-I of n values runs on an FFT of length 2(n - 1)
+    ok_len = (lambda n: n >= 2 and _smooth13(2 * (n - 1))) if rkind == 4 else _smooth13
+    if not all(ok_len(n) for n in size):
+        with pytest.raises(gb.HeffteError):
+            gb.rtransform(rkind, gb.box3d((0, 0, 0), [s - 1 for s in size]),
+                          gb.box3d((0, 0, 0), [s - 1 for s in size]))
+        return
     rng = np.random.default_rng(11 + sum(size))
     n = int(np.prod(size))
     x = rng.standard_normal(n).astype(rdt(prec))
-    ok = O.COS if rkind == 2 else O.SIN
+    ok = {2: O.COS, 3: O.SIN, 4: O.COS1}[rkind]
     for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 0, 1), (1, 2, 0))]:
         for reorder in (0, 1):
             opts = gb.plan_options.default()
