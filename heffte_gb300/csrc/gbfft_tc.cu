@@ -138,7 +138,7 @@ __device__ __forceinline__ void slice3(float2 x, uint32_t &s0, uint32_t &s1, uin
 // ---------------------------------------------------------------------------
 // tile geometry
 // ---------------------------------------------------------------------------
-constexpr int kThreads = 128;      // one warpgroup: warp w reads TMEM lanes 32w..32w+31
+constexpr int kThreads = 256;      // two warpgroups, one per MMA batch: warp w reads TMEM lanes 32(w%4)..+31
 constexpr int kTile = 4096;        // complex values per tile
 constexpr int kRows = kTile / 16;  // radix-16 butterflies per stage and tile
 constexpr int kBatches = kRows / 128;
@@ -148,6 +148,7 @@ constexpr int kChunk = 128 * 16;        // one K chunk (8 BF16) of all 128 rows 
 constexpr int kBatchCols = 128;         // TMEM columns of one batch: accumulators G_0, G_1, G_2 (32 each)
 constexpr uint32_t kTmemCols = kBatchCols * kBatches;
 static_assert(kBatches * 128 == kRows, "tile must hold whole MMA batches");
+static_assert(kThreads == kRows, "one thread per butterfly row, one warpgroup per MMA batch");
 static_assert(kTmemCols >= 32 && (kTmemCols & (kTmemCols - 1)) == 0, "TMEM allocation is a power of two >= 32");
 
 template<int N> struct TcShape {
@@ -196,7 +197,7 @@ __device__ __forceinline__ bool mma_wait(uint64_t *bar, uint32_t parity, int *st
 }
 
 template<int N, bool FWD, bool COLS>
-__global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
+__global__ void __launch_bounds__(kThreads, 2) k_tc_c2c(TcArgs const a){
     using Sh = TcShape<N>;
     constexpr int LT = Sh::LT, NR16 = Sh::NR16, PADN = Sh::PADN, R0 = Sh::R0;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -226,11 +227,10 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
     int const first16 = (R0 > 1) ? 1 : 0;
     uint32_t phase = 0;
     bool fail = false;
-    int rexp[kBatches];
     // The raw values of a tile, kPer per thread, are loaded into registers one
     // tile ahead: the loads of tile t+1 are in flight while the tensor-core
-    // stages of tile t run.  Value i of a thread is element e = tid + 128 i of
-    // the tile (r0 = 1), or input q of butterfly b = tid + 128 (i / r0) of
+    // stages of tile t run.  Value i of a thread is element e = tid + 256 i of
+    // the tile (r0 = 1), or input q of butterfly b = tid + 256 (i / r0) of
     // the leading radix-r0 stage (i % r0 = q).
     constexpr int kPer = kTile / kThreads;
     constexpr int NRr = N / R0;
@@ -270,15 +270,16 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
         }
         __syncthreads();
         if (tile + gridDim.x < a.ntiles) issue_loads(tile + gridDim.x);
-        // ---- radix-16 stages on the tensor cores
+        // ---- radix-16 stages on the tensor cores: warpgroup bb builds, and
+        // reads back, MMA batch bb (thread tid owns butterfly row tid)
         for (int s = first16; s < P.nstages; s++){
             Stage const S = P.st[s];
             bool const last = (s == P.nstages - 1);
-            // A rows: gather, twiddle, split
-            #pragma unroll
-            for (int bb = 0; bb < kBatches; bb++){
-                int row = bb * 128 + tid;
-                int l = COLS ? row % LT : row / NR16, j = COLS ? row / LT : row % NR16;
+            int const row = tid, bb = tid >> 7, r = tid & 127;
+            int const l = COLS ? row % LT : row / NR16, j = COLS ? row / LT : row % NR16;
+            int rexp;
+            {
+                // A row: gather, twiddle, slice
                 int k = j & (S.Ns - 1);
                 float2 x[16];
                 #pragma unroll
@@ -294,10 +295,9 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                 float mx = 0.f;
                 #pragma unroll
                 for (int q = 0; q < 16; q++) mx = fmaxf(mx, fmaxf(fabsf(x[q].x), fabsf(x[q].y)));
-                int e = row_exponent(mx);
-                rexp[bb] = e;
-                float const sc = pow2f(8 - e);
-                uint32_t rowaddr = a_base + bb * kAbytes + (tid >> 3) * 128 + (tid & 7) * 16;
+                rexp = row_exponent(mx);
+                float const sc = pow2f(8 - rexp);
+                uint32_t rowaddr = a_base + bb * kAbytes + (r >> 3) * 128 + (r & 7) * 16;
                 #pragma unroll
                 for (int c = 0; c < 4; c++){
                     uint32_t h[4], m[4], lo[4];
@@ -307,34 +307,36 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                     st_shared_v4(rowaddr + (4 + c) * kChunk, m[0], m[1], m[2], m[3]);
                     st_shared_v4(rowaddr + (8 + c) * kChunk, lo[0], lo[1], lo[2], lo[3]);
                 }
-                // this batch's MMAs run while the next batch is built
-                fence_proxy_async_smem();
-                tc_fence_before();
-                __syncthreads();
-                if (tid == 0){
-                    tc_fence_after();
+            }
+            fence_proxy_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0){
+                tc_fence_after();
+                #pragma unroll
+                for (int b2 = 0; b2 < kBatches; b2++){
                     #pragma unroll
                     for (int pr = 0; pr < 6; pr++){
                         #pragma unroll
                         for (int ks = 0; ks < 2; ks++){
-                            uint64_t ad = smem_desc(a_base + bb * kAbytes + (4 * term_a(pr) + 2 * ks) * kChunk, kChunk, 128);
+                            uint64_t ad = smem_desc(a_base + b2 * kAbytes + (4 * term_a(pr) + 2 * ks) * kChunk, kChunk, 128);
                             uint64_t bd = smem_desc(b_base + term_b(pr) * 2048 + 2 * ks * 512, 512, 128);
-                            mma_bf16(tbase + bb * kBatchCols + 32 * group_of(pr), ad, bd, kIdesc,
+                            mma_bf16(tbase + b2 * kBatchCols + 32 * group_of(pr), ad, bd, kIdesc,
                                      !(group_first(pr) && ks == 0));
                         }
                     }
-                    mma_commit(&bar[bb]);
+                    mma_commit(&bar[b2]);
                 }
-                __syncwarp();
             }
-            // D rows back from TMEM, batch by batch (every gather of the stage
-            // is done, so the tile can be overwritten)
-            bool ok = true;
-            #pragma unroll
-            for (int bb = 0; bb < kBatches; bb++){
-                ok = mma_wait(&bar[bb], phase, a.status) && ok;
-                tc_fence_after();
-                uint32_t const taddr = tbase + ((uint32_t)(warp * 32) << 16) + bb * kBatchCols;
+            // reconverge warp 0 before its other lanes enter the wait
+            __syncwarp();
+            bool const ok = mma_wait(&bar[bb], phase, a.status);
+            phase ^= 1;
+            tc_fence_after();
+            // D row back from TMEM (every gather of the stage is done, so the
+            // tile can be overwritten)
+            {
+                uint32_t const taddr = tbase + ((uint32_t)((warp & 3) * 32) << 16) + bb * kBatchCols;
                 float y[32];
                 {
                     uint32_t g1[32], g2[32];
@@ -348,20 +350,17 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                     uint32_t g0[32];
                     tmem_ld32(taddr, g0);
                     tmem_wait_ld();
-                    float const os = pow2f(rexp[bb] - 16) * (last && a.do_scale ? a.scale : 1.f);
+                    float const os = pow2f(rexp - 16) * (last && a.do_scale ? a.scale : 1.f);
                     #pragma unroll
                     for (int i = 0; i < 32; i++) y[i] = fmaf(y[i], 1.f / 512.f, __uint_as_float(g0[i])) * os;
                 }
-                int row = bb * 128 + tid;
-                int l = COLS ? row % LT : row / NR16, j = COLS ? row / LT : row % NR16;
                 if (last){
                     long long g = g0 + l;
                     if (g < a.G){
                         long long base = base_of(a.Lo, g);
                         #pragma unroll
-                        for (int q = 0; q < 16; q++){
+                        for (int q = 0; q < 16; q++)
                             a.out[base + (long long)(j + q * NR16) * a.Lo.estride] = make_float2(y[2 * q], y[2 * q + 1]);
-                        }
                     }
                 } else {
                     int hi = j >> (__ffs(S.Ns) - 1), k = j & (S.Ns - 1);
@@ -371,7 +370,6 @@ __global__ void __launch_bounds__(kThreads) k_tc_c2c(TcArgs const a){
                         D[sidx(PADN, l, ob + q * S.Ns)] = make_float2(y[2 * q], y[2 * q + 1]);
                 }
             }
-            phase ^= 1;
             tc_fence_before();
             if (__syncthreads_or(!ok)){ fail = true; break; }
         }
