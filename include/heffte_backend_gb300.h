@@ -1,7 +1,7 @@
 /*
  * heffte_backend_gb300.h - the reference-side binding: heFFTe backend tags
- * gb300 / gb300_cos / gb300_sin whose executors call libheffte_gb300 through
- * the C ABI of heffte_gb300.h.
+ * gb300 / gb300_cos / gb300_sin / gb300_cos1 whose executors call
+ * libheffte_gb300 through the C ABI of heffte_gb300.h.
  *
  * Include after heffte.h in a heFFTe build configured with Heffte_ENABLE_CUDA
  * (the tags reuse tag::gpu: device_vector, data_manipulator<tag::gpu>,
@@ -26,10 +26,13 @@ namespace backend {
     struct gb300_cos{};
     //! \brief Type-tag for the GB300 DST-II/III (cuFFT-sin conventions).
     struct gb300_sin{};
+    //! \brief Type-tag for the GB300 DCT-I (cuFFT-cos1 conventions).
+    struct gb300_cos1{};
 
     template<> struct is_enabled<gb300> : std::true_type{};
     template<> struct is_enabled<gb300_cos> : std::true_type{};
     template<> struct is_enabled<gb300_sin> : std::true_type{};
+    template<> struct is_enabled<gb300_cos1> : std::true_type{};
 
     template<> struct buffer_traits<gb300>{
         using location = tag::gpu;
@@ -43,13 +46,19 @@ namespace backend {
         using location = tag::gpu;
         template<typename T> using container = heffte::gpu::device_vector<T, data_manipulator<tag::gpu>>;
     };
+    template<> struct buffer_traits<gb300_cos1>{
+        using location = tag::gpu;
+        template<typename T> using container = heffte::gpu::device_vector<T, data_manipulator<tag::gpu>>;
+    };
 
     template<> struct uses_fft_types<gb300_cos> : std::false_type{};
     template<> struct uses_fft_types<gb300_sin> : std::false_type{};
+    template<> struct uses_fft_types<gb300_cos1> : std::false_type{};
 
     template<> inline std::string name<gb300>(){ return "gb300"; }
     template<> inline std::string name<gb300_cos>(){ return "gb300-cos-type-II"; }
     template<> inline std::string name<gb300_sin>(){ return "gb300-sin-type-II"; }
+    template<> inline std::string name<gb300_cos1>(){ return "gb300-cos-type-I"; }
 }
 
 namespace gb300 {
@@ -209,11 +218,16 @@ template<> struct one_dim_backend<backend::gb300_sin>{
     using executor = gb300_r2r_executor<HEFFTE_GB300_SIN>;
     using executor_r2c = void;
 };
+template<> struct one_dim_backend<backend::gb300_cos1>{
+    using executor = gb300_r2r_executor<HEFFTE_GB300_COS1>;
+    using executor_r2c = void;
+};
 
 // strided executors are the fast path: no transposes by default
 template<> struct default_plan_options<backend::gb300>{ static const bool use_reorder = false; };
 template<> struct default_plan_options<backend::gb300_cos>{ static const bool use_reorder = false; };
 template<> struct default_plan_options<backend::gb300_sin>{ static const bool use_reorder = false; };
+template<> struct default_plan_options<backend::gb300_cos1>{ static const bool use_reorder = false; };
 
 }
 
