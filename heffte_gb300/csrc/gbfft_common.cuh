@@ -57,6 +57,13 @@ struct Layout {
     long long count, dist, bstride, estride;
 };
 
+// Padded row pitch (in elements) of workspace-resident boxes whose fastest
+// extent e is odd: even (16-byte rows for complex<float>), and a multiple of
+// 8 (64-byte rows) from 65 elements on, where the c2r line tiles still fit.
+__host__ __device__ constexpr long long padded_pitch(long long e){
+    return (e >= 65) ? ((e + 7) / 8) * 8 : e + (e & 1);
+}
+
 __device__ __forceinline__ long long base_of(Layout const &L, long long g){
     return (g / L.count) * L.bstride + (g % L.count) * L.dist;
 }

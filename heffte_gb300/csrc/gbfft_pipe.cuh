@@ -76,11 +76,17 @@ __host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols){
     else { while (tpb * tt < 256) tpb *= 2; }
     while (tpb > 1 && tpb * tt > 512) tpb /= 2;
     while (tpb > 1 && 2 * (N + 2) * tpb * csize > 160 * 1024) tpb /= 2;
+    // and within the 227 KB of a CTA: two tile buffers (c2r lines at an even
+    // pitch: 2 (N/2+1) rounded up <= N + 4 values per unit) + the line exchange buffer
+    while (tpb > 1 && 2 * (N + 4) * tpb * csize + (cols ? 0 : tpb * pipe_padn(N) * csize) > 227 * 1024) tpb /= 2;
     return tpb;
 }
 // complex elements of one tile buffer (the c2r input tile holds N/2+1 rows of 2*TPB values)
+// (line tiles of the c2r kind keep their lines at a pitch of N/2+1, or at
+// the padded pitch of a workspace whose rows are padded_pitch(N/2+1))
+__host__ __device__ constexpr int pipe_c2r_pitch(int N){ return (int)padded_pitch(N / 2 + 1); }
 __host__ __device__ constexpr int pipe_tile_elems(int N, int tpb, int kind){
-    return (kind == PK_C2R_BWD) ? (N / 2 + 1) * 2 * tpb : N * tpb;
+    return (kind == PK_C2R_BWD) ? pipe_c2r_pitch(N) * 2 * tpb : N * tpb;
 }
 __host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind){
     int tpb = pipe_tpb(N, csize, cols);
@@ -100,6 +106,7 @@ struct PipeParams {
     int do_scale;
     int sine;
     int tswap;
+    int line_pitch;         // line tiles: input elements per line (LINE_LEN, or padded for c2r)
     int *status;
 };
 
@@ -249,7 +256,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         } else if constexpr (LOADER == LD_BULK){
             if (warp == 0 && lane == 0){
                 long long lines = ((long long)TPB * units_per < P.G - c0) ? (long long)TPB * units_per : (P.G - c0);
-                uint32_t bytes = (uint32_t)(lines * LINE_LEN * IN_ES);
+                uint32_t bytes = (uint32_t)(lines * P.line_pitch * IN_ES);
                 long long base = base_of_fast(Li, c0);
                 mbar_arrive_expect_tx(&bar[b], bytes);
                 bulk_g2s(dst, reinterpret_cast<unsigned char const*>(P.in) + base * IN_ES, bytes, &bar[b]);
@@ -383,7 +390,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
                 bool real_only = (pp == 0) || (2 * pp == N);
                 C xa, xb;
                 if (COLS){ xa = tb[pp * (2 * TPB) + 2 * loc]; xb = tb[pp * (2 * TPB) + 2 * loc + 1]; }
-                else { xa = tb[(2 * loc) * H + pp]; xb = tb[(2 * loc + 1) * H + pp]; }
+                else { xa = tb[(2 * loc) * P.line_pitch + pp]; xb = tb[(2 * loc + 1) * P.line_pitch + pp]; }
                 if (real_only){ xa.y = 0; xb.y = 0; }
                 if (cj){ xa.y = -xa.y; xb.y = -xb.y; }
                 C z; z.x = xa.x - xb.y; z.y = xa.y + xb.x;

@@ -20,6 +20,7 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     constexpr bool PAIRED = pipe_paired(KIND);
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
     constexpr int SMEM = pipe_smem(N, sizeof(C), COLS, KIND);
+    static_assert(SMEM <= 227 * 1024, "pipelined tile exceeds the shared memory of a CTA");
     constexpr int THREADS = pipe_threads(N, sizeof(C), COLS);
     constexpr int IN_ES = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) ? (int)sizeof(T) : (int)sizeof(C);
     constexpr int ROWS = (KIND == PK_C2R_BWD) ? N / 2 + 1 : N;
@@ -42,11 +43,17 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
             return false;
         P.tswap = swap;
     } else if constexpr (LOADER == LD_BULK){
-        if (Li.dist != LINE_LEN) return false;
-        if (blocks > 1 && Li.bstride != Li.count * LINE_LEN) return false;
-        if ((base & 15) || ((long long)a.G * LINE_LEN * IN_ES) % 16 != 0 ||
-            ((long long)TPB * UNITS * LINE_LEN * IN_ES) % 16 != 0)
+        // lines back to back, or (c2r) at the padded pitch of a workspace
+        long long pitch = LINE_LEN;
+        if (Li.dist != LINE_LEN){
+            if (KIND != PK_C2R_BWD || Li.dist != pipe_c2r_pitch(N)) return false;
+            pitch = Li.dist;
+        }
+        if (blocks > 1 && Li.bstride != Li.count * pitch) return false;
+        if ((base & 15) || ((long long)a.G * pitch * IN_ES) % 16 != 0 ||
+            ((long long)TPB * UNITS * pitch * IN_ES) % 16 != 0)
             return false;
+        P.line_pitch = (int)pitch;
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }

@@ -138,7 +138,7 @@ std::array<int, 3> order_with_first(std::array<int, 3> const &cur, int d){
 //   out_holds_inter: the output buffer has the element type of the intermediate data
 std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_box, Box3 const &dst_box,
                           Box3 const &inter_geom, bool reorder, bool out_holds_inter, bool in_aliases_out,
-                          int &work_buffers, int radix_policy, bool dct1 = false){
+                          int &work_buffers, int radix_policy, bool dct1 = false, bool pad_work = false){
     // drop length-1 complex passes (identity), keep at least one op to move
     // the data; a length-1 r2r transform is not the identity (REDFT10 of one
     // value is twice the value) and r2c/c2r change the element type
@@ -213,7 +213,8 @@ std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_b
                                 first.sbox.order != first.dbox.order;
     bool orders_kept = true;
     for (auto const &o : ops) orders_kept = orders_kept && (o.sbox.order == o.dbox.order);
-    bool x_is_out = !has_reshape && out_holds_inter && orders_kept && !(in_aliases_out && first_changes_layout);
+    bool x_is_out = !has_reshape && out_holds_inter && orders_kept && !(in_aliases_out && first_changes_layout) &&
+                    !pad_work;
     int cur_buf = B_IN;
     int used = 0;
     for (size_t i = 0; i < ops.size(); i++){
@@ -231,6 +232,18 @@ std::vector<Op> build_ops(std::vector<PassSpec> const &passes, Box3 const &src_b
         cur_buf = o.dst;
     }
     work_buffers = used;
+    // workspace-resident data with padded rows (padded_pitch): an odd extent
+    // of complex<float> rows (e.g. the 257 of a 512-point r2c box) gives row
+    // pitches that are not multiples of 16 bytes, which the tensor-memory-
+    // access loads of the column passes require
+    if (pad_work){
+        auto padded = [](Box3 b){ b.pitch0 = padded_pitch(b.size[b.order[0]]); return b; };
+        for (auto &o : ops){
+            if (o.type != Op::FFT) continue;
+            if (o.src == B_WA || o.src == B_WB) o.sbox = padded(o.sbox);
+            if (o.dst == B_WA || o.dst == B_WB) o.dbox = padded(o.dbox);
+        }
+    }
     return ops;
 }
 
@@ -283,6 +296,7 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         p->fwd = build_ops(fwd, inbox, outbox, inbox, reorder, true, false, wf, knobs.radix_policy, dct1);
         p->fwd_alias = p->fwd;
         p->bwd = build_ops(bwd, outbox, inbox, inbox, reorder, true, false, wb, knobs.radix_policy, dct1);
+        p->work_buf_elems = inbox.count();
         p->work_elems = std::max(wf, wb) * inbox.count();
         double n = (double)inbox.count();
         // include/heffte_fft3d.h:635-650: 1/(64 N) for the cos/sin tags, 1/(64 prod(n_i - 1)) for DCT-I
@@ -294,10 +308,21 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         for (int i = 0; i < 3; i++) if (io[i] != r2c_dir) fwd.push_back({K_C2C_F, io[i]});
         for (int i = 0; i < 3; i++) if (oo[i] != r2c_dir) bwd.push_back({K_C2C_B, oo[i]});
         bwd.push_back({K_C2R, r2c_dir});
-        p->fwd = build_ops(fwd, inbox, outbox, cgeom, reorder, true, false, wf, knobs.radix_policy);
-        p->fwd_alias = build_ops(fwd, inbox, outbox, cgeom, reorder, true, true, wfa, knobs.radix_policy);
-        p->bwd = build_ops(bwd, outbox, inbox, cgeom, reorder, false, false, wb, knobs.radix_policy);
-        p->work_elems = std::max(std::max(wf, wfa), wb) * cgeom.count();
+        // the complex intermediate goes through a padded workspace when its
+        // fastest extent is odd (plans without reshapes)
+        bool pad_f = !reorder && (cgeom.size[io[0]] % 2 == 1);
+        bool pad_b = !reorder && (cgeom.size[oo[0]] % 2 == 1);
+        p->fwd = build_ops(fwd, inbox, outbox, cgeom, reorder, true, false, wf, knobs.radix_policy, false, pad_f);
+        p->fwd_alias = build_ops(fwd, inbox, outbox, cgeom, reorder, true, true, wfa, knobs.radix_policy, false, pad_f);
+        p->bwd = build_ops(bwd, outbox, inbox, cgeom, reorder, false, false, wb, knobs.radix_policy, false, pad_b);
+        long long per = cgeom.count();
+        for (auto const *ops : {&p->fwd, &p->fwd_alias, &p->bwd})
+            for (auto const &o : *ops){
+                if (o.src == B_WA || o.src == B_WB) per = std::max(per, o.sbox.alloc_count());
+                if (o.dst == B_WA || o.dst == B_WB) per = std::max(per, o.dbox.alloc_count());
+            }
+        p->work_buf_elems = per;
+        p->work_elems = std::max(std::max(wf, wfa), wb) * per;
         p->scale_factor = 1.0 / (double)inbox.count();
     }
     return p;
@@ -335,7 +360,7 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
     bool alias = (in == out);
     std::vector<Op> const &ops = forward ? (alias ? fwd_alias : fwd) : bwd;
     // the workspace: 2 halves of work_elems/2 ... one box each
-    long long per_buf = (kind == PK_R2C) ? inbox.r2c(r2c_dir).count() : inbox.count();
+    long long per_buf = work_buf_elems;
     size_t need = (size_t)work_elems * work_es;
     char *wbase = reinterpret_cast<char*>(work);
     if (need > 0 && !wbase){

@@ -10,12 +10,16 @@ namespace gbfft {
 struct Box3 {
     std::array<long long, 3> lo{0, 0, 0}, hi{-1, -1, -1}, size{0, 0, 0};
     std::array<int, 3> order{0, 1, 2};
+    long long pitch0 = 0;   // padded extent of the fastest dimension order[0] (0: dense)
     Box3() = default;
     Box3(std::array<long long, 3> l, std::array<long long, 3> h, std::array<int, 3> o) : lo(l), hi(h), order(o){
         for (int i = 0; i < 3; i++) size[i] = hi[i] - lo[i] + 1;
     }
     bool empty() const { return size[0] <= 0 || size[1] <= 0 || size[2] <= 0; }
     long long count() const { return empty() ? 0 : size[0] * size[1] * size[2]; }
+    long long p0() const { return pitch0 > 0 ? pitch0 : size[order[0]]; }
+    // elements of the array holding the box (with the padding)
+    long long alloc_count() const { return empty() ? 0 : p0() * size[order[1]] * size[order[2]]; }
     long long osize(int d) const { return size[order[d]]; }
     int find_order(int dir) const { return (dir == order[0]) ? 0 : ((dir == order[1]) ? 1 : 2); }
     // box3d::r2c (heffte_geometry.h:85-93)
@@ -23,14 +27,15 @@ struct Box3 {
         Box3 b = *this;
         b.hi[dim] = lo[dim] + size[dim] / 2;
         b.size[dim] = b.hi[dim] - b.lo[dim] + 1;
+        b.pitch0 = 0;
         return b;
     }
-    Box3 with_order(std::array<int, 3> o) const { Box3 b = *this; b.order = o; return b; }
+    Box3 with_order(std::array<int, 3> o) const { Box3 b = *this; b.order = o; b.pitch0 = 0; return b; }
     std::array<long long, 3> strides() const {
         std::array<long long, 3> s{};
         s[order[0]] = 1;
-        s[order[1]] = size[order[0]];
-        s[order[2]] = size[order[0]] * size[order[1]];
+        s[order[1]] = p0();
+        s[order[2]] = p0() * size[order[1]];
         return s;
     }
 };
@@ -105,6 +110,7 @@ struct Plan3D {
     cudaStream_t stream = nullptr;
     std::vector<Op> fwd, fwd_alias, bwd;
     long long work_elems = 0;     // workspace in output-type elements (complex for c2c/r2c)
+    long long work_buf_elems = 0; // elements of one of the (up to two) workspace buffers
     double scale_factor = 1.0;    // "full" factor
     void *cached_work = nullptr;  // lazily allocated when the caller passes no workspace
     size_t cached_bytes = 0;
