@@ -288,6 +288,7 @@ def ours(args, rank, world, local_rank):
                    "l2": f"inputs {N * esize / 2**30:.2f} GiB > 129 MB L2 (no flush needed)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
+                     "peak_nominal": NOMINAL_HBM_GBS, "frac_nominal": achieved / NOMINAL_HBM_GBS,
                      # DRAM read+write bytes per launch of the column pass kernel, from the ncu
                      # launch list of this command (profiles/k_pipe_c2c_512cube_fp32.md)
                      "traffic": 2.083e9 if (n == 512 and prec == 0) else None,
@@ -307,21 +308,32 @@ def ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
-def fp64_check(gb, box, x, stream, forms):
+NOMINAL_HBM_GBS = 7900.0   # GB300 HBM3e nominal bandwidth
+
+
+def fp64_check(gb, box, x, stream, forms, kind="c2c"):
     """rel-L2 of the forward transform of x by each plan in `forms` against this
-    library's complex<double> transform of the same input (the FP64 path the
-    parity tests hold to 1e-12 of the FP64 oracle)."""
+    library's double-precision transform of the same input (the FP64 path the
+    parity tests hold to 1e-12 of the FP64 oracle); kind c2c, r2c or cos."""
     import torch
-    p64 = gb.fft3d(box, box, stream=stream)
-    x64 = x.to(torch.complex128)
-    y64 = torch.empty_like(x64)
+    if kind == "c2c":
+        p64 = gb.fft3d(box, box, stream=stream)
+        x64 = x.to(torch.complex128)
+    elif kind == "r2c":
+        p64 = gb.fft3d_r2c(box, box.r2c(0), 0, stream=stream)
+        x64 = x.to(torch.float64)
+    else:
+        p64 = gb.rtransform(gb.kind.cos, box, box, stream=stream)
+        x64 = x.to(torch.float64)
+    odt = torch.complex128 if kind != "cos" else torch.float64
+    y64 = torch.empty(p64.size_outbox(), dtype=odt, device=x.device)
     p64.forward(x64, y64)
     del x64
     out = {}
     for name, p in forms.items():
-        y = torch.empty_like(x)
+        y = torch.empty(p.size_outbox(), dtype=torch.complex64 if kind != "cos" else torch.float32, device=x.device)
         p.forward(x, y)
-        out[name] = float((torch.linalg.vector_norm(y.to(torch.complex128) - y64) / torch.linalg.vector_norm(y64)).item())
+        out[name] = float((torch.linalg.vector_norm(y.to(odt) - y64) / torch.linalg.vector_norm(y64)).item())
         del y
     return out
 
@@ -382,6 +394,8 @@ WORKLOADS = {
     "batch256tuned": ("batch", "tuned", 0),
     # the same boxes as a loop over one fft3d_r2c plan per box (how the reference runs them)
     "batch256loop": ("batch", "loop", 0),
+    # learned plan selection on the 2000 measured shapes (tests/golden/selector_timings.npz)
+    "selector2000": ("selector", None, 0),
 }
 
 BATCH_SIDES = [16, 24, 32, 40, 48, 64, 80, 96, 128]
@@ -482,10 +496,45 @@ def algorithmic_bytes(kind, size, prec):
     return 3 * 2 * N * rs
 
 
+def run_selector_workload(name):
+    """Trains the selector (this library's CUDA kernels) on 80% of the measured
+    shapes, and reports its held-out regret against exhaustive search, the
+    default plan's and the best fixed candidate's, the training time and the
+    time of one selection."""
+    import time
+    import torch
+    from heffte_gb300 import selector
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "selector_timings.npz"))
+    X, T = d["X"], selector.filled(d["T"])
+    idx = np.random.default_rng(0).permutation(len(X))
+    tr, te = idx[:int(0.8 * len(X))], idx[int(0.8 * len(X)):]
+    net = selector.Selector(hidden=64, seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = net.train(X[tr], selector.targets(T[tr]), steps=4000, lr=2e-3)
+    train_s = time.perf_counter() - t0
+    choice = net.choose(X[te])
+    fixed = int(np.argmin(np.log(T[tr] / T[tr].min(axis=1, keepdims=True)).mean(axis=0)))
+    shapes = selector.sample_shapes(len(X), seed=int(d["seed"]))
+    t0 = time.perf_counter()
+    for i in te[:100]:
+        net.select(*shapes[i])
+    sel_us = (time.perf_counter() - t0) / 100 * 1e6
+    return {"workload": name, "shapes": int(len(X)), "train_shapes": int(len(tr)), "heldout_shapes": int(len(te)),
+            "regret_selector": selector.regret(T[te], choice),
+            "regret_default_plan": selector.regret(T[te], np.zeros(len(te), dtype=int)),
+            "regret_best_fixed_candidate": selector.regret(T[te], np.full(len(te), fixed)),
+            "train_s": train_s, "train_steps": 4000, "final_loss": loss, "select_us": sel_us,
+            "network": "18-64-64-16 ReLU, FP32, full-batch Adam (CUDA kernels of this library)",
+            "dataset_device": str(d["device"])}
+
+
 def run_workload(name, steps, warmup):
     import torch
     import heffte_gb300 as gb
     kind, size, prec = WORKLOADS[name][:3]
+    if kind == "selector":
+        return run_selector_workload(name)
     tc = len(WORKLOADS[name]) > 3 and WORKLOADS[name][3]
     if kind == "batch":
         cache = "loop" if size == "loop" else None
@@ -540,9 +589,9 @@ def run_workload(name, steps, warmup):
     peak, _ = peaks()
     out = {"workload": name, "ms_per_step": ms, "gflops": 2 * flops_per_transform(N) / (ms / 1e3) / 1e9,
            "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak, "roundtrip_max_abs": err}
-    if kind == "c2c" and prec == 0:
+    if prec == 0:
         del y, z, work
-        out["rel_l2_forward_vs_fp64"] = fp64_check(gb, box, x, stream, {"p": plan})["p"]
+        out["rel_l2_forward_vs_fp64"] = fp64_check(gb, box, x, stream, {"p": plan}, kind)["p"]
     if tc:
         out["tensor_cores"] = True
     return out

@@ -212,3 +212,17 @@ def regret(T, choice):
     T = filled(T)
     t = T[np.arange(len(T)), choice]
     return float(np.mean(t / T.min(axis=1) - 1.0))
+
+
+def best_candidate(size, tkind, prec, net=None, reps=3):
+    """The candidate plan of one shape: the network's pick, or, without a
+    network (the fallback), the fastest of all 16 by exhaustive timing."""
+    if net is not None:
+        return net.select(tuple(size), tkind, prec)
+    _, T = measure([(tuple(size), tkind, prec)], reps=reps)
+    return int(np.nanargmin(T[0]))
+
+
+def plan_for(size, tkind, prec, net=None, stream=None):
+    """A plan of the shape built with the chosen candidate's options and knobs."""
+    return make_plan(tuple(size), tkind, prec, best_candidate(size, tkind, prec, net), stream)

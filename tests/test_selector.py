@@ -171,3 +171,25 @@ def test_selector_regret_and_gain(gb):
     assert r_sel <= 0.05
     assert r_sel < r_default
     assert r_sel <= r_fixed
+
+
+@pytest.mark.gpu
+def test_plan_for_with_and_without_network(gb):
+    """plan_for uses the network's pick, or exhaustive timing without one; both
+    plans compute the same transform (numerics are untouched by the choice)."""
+    import torch
+    from heffte_gb300 import selector
+    size, tkind, prec = (48, 40, 36), gb.kind.c2c, 0
+    rng = np.random.default_rng(5)
+    n = int(np.prod(size))
+    x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex64)
+    from oracle import heffte_oracle as O
+    ref = O.fft3d_c2c(x, size)
+    c = selector.best_candidate(size, tkind, prec)
+    assert 0 <= c < 16
+    net = selector.Selector(hidden=NH, seed=1)
+    for p in (selector.plan_for(size, tkind, prec), selector.plan_for(size, tkind, prec, net)):
+        xin = torch.from_numpy(x).cuda()
+        y = torch.empty_like(xin)
+        p.forward(xin, y)
+        assert O.rel_l2(y.cpu().numpy(), ref) <= 1e-6
