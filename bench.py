@@ -161,6 +161,17 @@ def reference_arm(args, rank, world):
 # --------------------------------------------------------------------------
 # our arm
 # --------------------------------------------------------------------------
+def combine_replicas(ms_step, world, flops_per_step, dist=None, device="cpu"):
+    """Replicas only (the single-rank path does not shard): the step time is
+    the maximum over ranks and the value the whole job's work (every replica's
+    steps) over that time.  dist: torch.distributed (None on one rank)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([ms_step], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    return ms_step, world * flops_per_step / (ms_step / 1e3) / 1e9
+
 def ours(args, rank, world, local_rank):
     import torch
     import heffte_gb300 as gb
@@ -214,11 +225,7 @@ def ours(args, rank, world, local_rank):
         dist.barrier()
     clk = clocks.stop()
     ms_step = ms / args.steps
-    if dist:
-        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * 2 * flops_per_transform(N) / (ms_step / 1e3) / 1e9
+    ms_step, value = combine_replicas(ms_step, world, 2 * flops_per_transform(N), dist, "cuda")
 
     # dominant kernel: one strided pass (k_c2c column layout, the y and z
     # passes) and the contiguous x pass, each timed on its own with events
