@@ -107,6 +107,7 @@ struct PipeParams {
     int sine;
     int tswap;
     int line_pitch;         // line tiles: input elements per line (LINE_LEN, or padded for c2r)
+    int bulk_store;         // c2c line tiles: results staged in the tile buffer, one bulk store per tile
     int *status;
 };
 
@@ -255,6 +256,8 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             }
         } else if constexpr (LOADER == LD_BULK){
             if (warp == 0 && lane == 0){
+                // the buffer's previous tile may still be read by its bulk store
+                if (P.bulk_store) bulk_wait_read<0>();
                 long long lines = ((long long)TPB * units_per < P.G - c0) ? (long long)TPB * units_per : (P.G - c0);
                 uint32_t bytes = (uint32_t)(lines * P.line_pitch * IN_ES);
                 long long base = base_of_fast(Li, c0);
@@ -307,7 +310,10 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             __syncthreads();
         } else {
             bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0, P.status);
-            if (__syncthreads_or(!ok)) return;
+            if (__syncthreads_or(!ok)){
+                if (P.bulk_store && tid == 0) bulk_wait<0>();
+                return;
+            }
             if (b) ph1 ^= 1; else ph0 ^= 1;
         }
 
@@ -340,8 +346,22 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         if constexpr (KIND == PK_C2C_FWD || KIND == PK_C2C_BWD){
             auto ld0 = [&](int p) -> C { return COLS ? tb[p * TPB + loc] : tb[loc * N + p]; };
             C *out = reinterpret_cast<C*>(P.out);
-            auto st = [&](int p, C x){ if (va) out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
-            pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            if (!COLS && LOADER == LD_BULK && P.bulk_store){
+                // the last stage writes the tile buffer (read only by stage 0),
+                // one thread stores the whole tile with a bulk copy
+                auto st = [&](int p, C x){ tb[loc * N + p] = P.do_scale ? cscale(x, sc) : x; };
+                pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+                fence_proxy_async_smem();
+                __syncthreads();
+                if (tid == 0){
+                    long long lines = ((long long)TPB < P.G - c0) ? (long long)TPB : (P.G - c0);
+                    bulk_s2g(out + base_of_fast(Lo, c0), tb, (uint32_t)(lines * N * sizeof(C)));
+                    bulk_commit();
+                }
+            } else {
+                auto st = [&](int p, C x){ if (va) out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
+                pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            }
         } else if constexpr (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD){
             auto ld0 = [&](int p) -> C {
                 int n = p;
@@ -434,6 +454,8 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         }
         __syncthreads();
     }
+    // the last bulk stores must be complete before the CTA's shared memory goes
+    if (LOADER == LD_BULK && P.bulk_store && tid == 0) bulk_wait<0>();
 }
 
 } // namespace gbfft

@@ -54,6 +54,12 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
             ((long long)TPB * UNITS * pitch * IN_ES) % 16 != 0)
             return false;
         P.line_pitch = (int)pitch;
+        // c2c line tiles whose output lines are back to back: one bulk store per tile
+        Layout const &Lo = a.Lo;
+        uintptr_t obase = reinterpret_cast<uintptr_t>(a.out);
+        if ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && N >= 32 && Lo.estride == 1 && Lo.dist == N &&
+            (a.G <= Lo.count || Lo.bstride == Lo.count * N) && (obase & 15) == 0)
+            P.bulk_store = 1;
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }

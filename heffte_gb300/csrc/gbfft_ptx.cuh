@@ -77,4 +77,20 @@ __device__ __forceinline__ void bulk_g2s(void *dst_smem, void const *src_gmem, u
                  :: "r"(smem_u32(dst_smem)), "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
+// 1-D bulk copy shared -> global, tracked by bulk groups of the issuing
+// thread.  dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void bulk_s2g(void *dst_gmem, void const *src_smem, uint32_t bytes){
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                 :: "l"(dst_gmem), "r"(smem_u32(src_smem)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit(){ asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// until at most NG of this thread's bulk groups still read their shared source
+template<int NG> __device__ __forceinline__ void bulk_wait_read(){
+    asm volatile("cp.async.bulk.wait_group.read %0;" :: "n"(NG) : "memory");
+}
+// until at most NG of this thread's bulk groups are incomplete
+template<int NG> __device__ __forceinline__ void bulk_wait(){
+    asm volatile("cp.async.bulk.wait_group %0;" :: "n"(NG) : "memory");
+}
+
 } // namespace gbfft
