@@ -161,6 +161,68 @@ def reference_arm(args, rank, world):
 # --------------------------------------------------------------------------
 # our arm
 # --------------------------------------------------------------------------
+def e2e_streamed(gb, box, prec, cdt, N, x, args):
+    """Per-step time of the streamed end-to-end loop (see the caller) and the
+    largest round-trip error of the results that came back to the host."""
+    import torch
+    s_cmp, s_h2d, s_d2h = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    plan = gb.fft3d(box, box, stream=s_cmp)
+    hx = torch.empty(N, dtype=cdt, pin_memory=True)
+    hx.copy_(x.cpu())
+    hz = [torch.empty(N, dtype=cdt, pin_memory=True) for _ in range(2)]
+    xin = [torch.empty_like(x) for _ in range(2)]
+    yb = [torch.empty_like(x) for _ in range(2)]
+    zb = [torch.empty_like(x) for _ in range(2)]
+    work = torch.empty(max(plan.size_workspace(), 1), dtype=cdt, device="cuda")
+    h2d_done = [torch.cuda.Event() for _ in range(2)]
+    cmp_done = [torch.cuda.Event() for _ in range(2)]
+    d2h_done = [torch.cuda.Event() for _ in range(2)]
+    used = [False, False]
+
+    def step(k):
+        b = k % 2
+        if used[b]:
+            s_h2d.wait_event(cmp_done[b])      # xin[b] was read by step k-2
+        with torch.cuda.stream(s_h2d):
+            xin[b].copy_(hx, non_blocking=True)
+            h2d_done[b].record(s_h2d)
+        s_cmp.wait_event(h2d_done[b])
+        if used[b]:
+            s_cmp.wait_event(d2h_done[b])      # zb[b] was read back by step k-2
+        plan.forward_ptr(prec, xin[b].data_ptr(), yb[b].data_ptr(), work.data_ptr(), gb.scale.full)
+        plan.backward_ptr(prec, yb[b].data_ptr(), zb[b].data_ptr(), work.data_ptr(), gb.scale.none)
+        cmp_done[b].record(s_cmp)
+        s_d2h.wait_event(cmp_done[b])
+        with torch.cuda.stream(s_d2h):
+            hz[b].copy_(zb[b], non_blocking=True)
+            d2h_done[b].record(s_d2h)
+        used[b] = True
+
+    for k in range(2):
+        step(k)
+    torch.cuda.synchronize()
+    # three timed runs of e_steps steps each; the host link's throughput
+    # varies from run to run, the median is reported
+    e_steps = max(4, min(args.steps, 12))
+    cur = torch.cuda.current_stream()
+    runs, k = [], 2
+    for _ in range(3):
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(cur)
+        for s_ in (s_cmp, s_h2d, s_d2h):
+            s_.wait_event(start)
+        for _ in range(e_steps):
+            step(k)
+            k += 1
+        for s_ in (s_cmp, s_h2d, s_d2h):
+            cur.wait_stream(s_)
+        end.record(cur)
+        torch.cuda.synchronize()
+        runs.append(start.elapsed_time(end) / e_steps)
+    rt = max(float(np.abs(h.numpy() - hx.numpy()).max()) for h in hz)
+    return float(np.median(runs)), rt, runs
+
+
 def combine_replicas(ms_step, world, flops_per_step, dist=None, device="cpu"):
     """Replicas only (the single-rank path does not shard): the step time is
     the maximum over ranks and the value the whole job's work (every replica's
@@ -248,30 +310,13 @@ def ours(args, rank, world, local_rank):
     achieved = pass_bytes / (per_launch[dom] / 1e3) / 1e9
     step_bytes = 6 * pass_bytes   # algorithmic: 3 passes x read+write, forward and backward
 
-    # end-to-end through the C ABI with host buffers: H2D input, fwd+bwd, D2H result
-    hx = torch.empty(N, dtype=cdt, pin_memory=True)
-    hx.copy_(x.cpu())
-    hz = torch.empty(N, dtype=cdt, pin_memory=True)
-    xin = torch.empty_like(x)
-    for _ in range(2):
-        xin.copy_(hx, non_blocking=True)
-        plan.forward_ptr(prec, xin.data_ptr(), y.data_ptr(), work.data_ptr(), gb.scale.full)
-        plan.backward_ptr(prec, y.data_ptr(), z.data_ptr(), work.data_ptr(), gb.scale.none)
-        hz.copy_(z, non_blocking=True)
-    torch.cuda.synchronize()
-    e_steps = max(3, min(args.steps, 10))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e_steps):
-        xin.copy_(hx, non_blocking=True)
-        plan.forward_ptr(prec, xin.data_ptr(), y.data_ptr(), work.data_ptr(), gb.scale.full)
-        plan.backward_ptr(prec, y.data_ptr(), z.data_ptr(), work.data_ptr(), gb.scale.none)
-        hz.copy_(z, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e_steps
+    # end-to-end through the C ABI with host buffers, every step: H2D of its
+    # input from pinned memory, forward(scale::full) + backward, D2H of its
+    # result.  Streamed: step k's H2D (copy stream) and step k-1's D2H (a
+    # second copy stream) run while step k-1 / k compute on the plan's stream
+    # (two device buffer sets, events order every reuse of a buffer).
+    e2e_ms, rt_host, e2e_runs = e2e_streamed(gb, box, prec, cdt, N, x, args)
     e2e_val = world * 2 * flops_per_transform(N) / (e2e_ms / 1e3) / 1e9
-    rt_host = float(np.abs(hz.numpy() - hx.numpy()).max())
 
     tc = tensor_core_form(gb, box, x, y, z, work, stream, args, ms_step, world) if prec == 0 else None
 
@@ -306,7 +351,10 @@ def ours(args, rank, world, local_rank):
                      "step_frac": step_bytes / (ms_step / 1e3) / 1e9 / peak},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "GFLOP/s", "h2d_bytes_per_step": N * esize, "d2h_bytes_per_step": N * esize,
-                "ms_per_step": e2e_ms, "api": "heffte_gb300_forward/backward (C ABI), pinned host buffers"},
+                "ms_per_step": e2e_ms, "api": "heffte_gb300_forward/backward (C ABI), pinned host buffers",
+                "pipeline": "streamed: H2D of step k and D2H of step k-1 overlap the plan's compute "
+                            "(copy streams + plan stream, two device buffer sets)",
+                "ms_per_step_runs": e2e_runs},
         "gpu_launches": 6 * args.steps,
         "clocks": clk,
         "accuracy": {"roundtrip_max_abs": rt_err, "roundtrip_max_abs_e2e": rt_host},
