@@ -85,8 +85,10 @@ __host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols){
 // (line tiles of the c2r kind keep their lines at a pitch of N/2+1, or at
 // the padded pitch of a workspace whose rows are padded_pitch(N/2+1))
 __host__ __device__ constexpr int pipe_c2r_pitch(int N){ return (int)padded_pitch(N / 2 + 1); }
+// (an r2c tile buffer also stages the tile's complex output lines at that pitch)
 __host__ __device__ constexpr int pipe_tile_elems(int N, int tpb, int kind){
-    return (kind == PK_C2R_BWD) ? pipe_c2r_pitch(N) * 2 * tpb : N * tpb;
+    return (kind == PK_C2R_BWD || kind == PK_R2C_FWD)
+           ? ((pipe_c2r_pitch(N) * 2 * tpb > N * tpb) ? pipe_c2r_pitch(N) * 2 * tpb : N * tpb) : N * tpb;
 }
 __host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind){
     int tpb = pipe_tpb(N, csize, cols);
@@ -382,12 +384,32 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             if constexpr (KIND == PK_R2C_FWD){
                 C *out = reinterpret_cast<C*>(P.out);
                 T h = (T)0.5 * (P.do_scale ? sc : (T)1);
-                for (int k = t; k <= N / 2; k += TT){
-                    C zk = xch[xi(k)], zn = xch[xi((k == 0) ? 0 : N - k)];
-                    C xa; xa.x = h * (zk.x + zn.x); xa.y = h * (zk.y - zn.y);
-                    C xb; xb.x = h * (zk.y + zn.y); xb.y = -h * (zk.x - zn.x);
-                    if (va) out[oa + k * oes] = xa;
-                    if (vb) out[obb + k * oes] = xb;
+                if (!COLS && LOADER == LD_BULK && P.bulk_store){
+                    // output lines staged in the tile buffer (its real input was
+                    // read by stage 0) at the output pitch, one bulk store
+                    long long const SP = Lo.dist;
+                    for (int k = t; k <= N / 2; k += TT){
+                        C zk = xch[xi(k)], zn = xch[xi((k == 0) ? 0 : N - k)];
+                        C xa; xa.x = h * (zk.x + zn.x); xa.y = h * (zk.y - zn.y);
+                        C xb; xb.x = h * (zk.y + zn.y); xb.y = -h * (zk.x - zn.x);
+                        tb[(2 * loc) * SP + k] = xa;
+                        tb[(2 * loc + 1) * SP + k] = xb;
+                    }
+                    fence_proxy_async_smem();
+                    __syncthreads();
+                    if (tid == 0){
+                        long long lines = ((long long)TPB * 2 < P.G - c0) ? (long long)TPB * 2 : (P.G - c0);
+                        bulk_s2g(out + base_of_fast(Lo, c0), tb, (uint32_t)(lines * SP * sizeof(C)));
+                        bulk_commit();
+                    }
+                } else {
+                    for (int k = t; k <= N / 2; k += TT){
+                        C zk = xch[xi(k)], zn = xch[xi((k == 0) ? 0 : N - k)];
+                        C xa; xa.x = h * (zk.x + zn.x); xa.y = h * (zk.y - zn.y);
+                        C xb; xb.x = h * (zk.y + zn.y); xb.y = -h * (zk.x - zn.x);
+                        if (va) out[oa + k * oes] = xa;
+                        if (vb) out[obb + k * oes] = xb;
+                    }
                 }
             } else {
                 T *out = reinterpret_cast<T*>(P.out);
@@ -418,11 +440,29 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             };
             T *out = reinterpret_cast<T*>(P.out);
             T s = P.do_scale ? sc : (T)1;
-            auto st = [&](int p, C x){
-                if (va) out[oa + p * oes] = x.x * s;
-                if (vb) out[obb + p * oes] = x.y * s;
-            };
-            pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            if (!COLS && LOADER == LD_BULK && P.bulk_store){
+                // the real output lines staged in the tile buffer (its complex
+                // input was read by stage 0), one bulk store
+                T *stg = reinterpret_cast<T*>(tb);
+                auto st = [&](int p, C x){
+                    stg[(2 * loc) * N + p] = x.x * s;
+                    stg[(2 * loc + 1) * N + p] = x.y * s;
+                };
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+                fence_proxy_async_smem();
+                __syncthreads();
+                if (tid == 0){
+                    long long lines = ((long long)TPB * 2 < P.G - c0) ? (long long)TPB * 2 : (P.G - c0);
+                    bulk_s2g(out + base_of_fast(Lo, c0), stg, (uint32_t)(lines * N * sizeof(T)));
+                    bulk_commit();
+                }
+            } else {
+                auto st = [&](int p, C x){
+                    if (va) out[oa + p * oes] = x.x * s;
+                    if (vb) out[obb + p * oes] = x.y * s;
+                };
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            }
         } else {
             // PK_R2R_BWD: V[k] = 2 exp(i pi k / 2N) (Y[k] - i Y[N-k]), two lines per FFT
             C const *rtw = reinterpret_cast<C const*>(P.rtw);

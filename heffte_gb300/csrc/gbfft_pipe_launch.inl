@@ -60,6 +60,16 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
         if ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && N >= 32 && Lo.estride == 1 && Lo.dist == N &&
             (a.G <= Lo.count || Lo.bstride == Lo.count * N) && (obase & 15) == 0)
             P.bulk_store = 1;
+        // r2c: complex output lines (N/2+1, or the padded pitch) back to back;
+        // c2r: real output lines back to back; every tile's bytes a multiple of 16
+        constexpr int H2 = N / 2 + 1;
+        if (KIND == PK_R2C_FWD && N >= 32 && Lo.estride == 1 && (Lo.dist == H2 || Lo.dist == pipe_c2r_pitch(N)) &&
+            (a.G <= Lo.count || Lo.bstride == Lo.count * Lo.dist) && (obase & 15) == 0 &&
+            (a.G % 2 == 0 || Lo.dist % 2 == 0))
+            P.bulk_store = 1;
+        if (KIND == PK_C2R_BWD && N >= 32 && Lo.estride == 1 && Lo.dist == N &&
+            (a.G <= Lo.count || Lo.bstride == Lo.count * N) && (obase & 15) == 0)
+            P.bulk_store = 1;
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }
