@@ -415,14 +415,33 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
                 T *out = reinterpret_cast<T*>(P.out);
                 C const *rtw = reinterpret_cast<C const*>(P.rtw);
                 T s = P.do_scale ? sc : (T)1;
+                // bulk store: the real output lines staged in the tile buffer
+                // (its real input was read by stage 0)
+                bool const stage = !COLS && LOADER == LD_BULK && P.bulk_store;
+                T *stg = reinterpret_cast<T*>(tb);
                 for (int k = t; k < N; k += TT){
                     C zk = xch[xi(k)], zn = xch[xi((k == 0) ? 0 : N - k)];
                     C w = __ldg(rtw + k);
                     T ax = zk.x + zn.x, ay = zk.y - zn.y;
                     T bx = zk.y + zn.y, by = -(zk.x - zn.x);
                     int ko = sine ? (N - 1 - k) : k;
-                    if (va) out[oa + ko * oes] = (w.x * ax - w.y * ay) * s;
-                    if (vb) out[obb + ko * oes] = (w.x * bx - w.y * by) * s;
+                    T ya = (w.x * ax - w.y * ay) * s, yb = (w.x * bx - w.y * by) * s;
+                    if (stage){
+                        stg[(2 * loc) * N + ko] = ya;
+                        stg[(2 * loc + 1) * N + ko] = yb;
+                    } else {
+                        if (va) out[oa + ko * oes] = ya;
+                        if (vb) out[obb + ko * oes] = yb;
+                    }
+                }
+                if (stage){
+                    fence_proxy_async_smem();
+                    __syncthreads();
+                    if (tid == 0){
+                        long long lines = ((long long)TPB * 2 < P.G - c0) ? (long long)TPB * 2 : (P.G - c0);
+                        bulk_s2g(out + base_of_fast(Lo, c0), stg, (uint32_t)(lines * N * sizeof(T)));
+                        bulk_commit();
+                    }
                 }
             }
         } else if constexpr (KIND == PK_C2R_BWD){
@@ -484,13 +503,33 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             };
             T *out = reinterpret_cast<T*>(P.out);
             T s = P.do_scale ? sc : (T)1;
-            auto st = [&](int n, C x){
-                int m = (2 * n < N) ? 2 * n : 2 * (N - 1 - n) + 1;
-                T sg = (sine && (m & 1)) ? -s : s;
-                if (va) out[oa + m * oes] = x.x * sg;
-                if (vb) out[obb + m * oes] = x.y * sg;
-            };
-            pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            if (!COLS && LOADER == LD_BULK && P.bulk_store){
+                // the real output lines staged in the tile buffer (its real
+                // input was read by stage 0), one bulk store
+                T *stg = reinterpret_cast<T*>(tb);
+                auto st = [&](int n, C x){
+                    int m = (2 * n < N) ? 2 * n : 2 * (N - 1 - n) + 1;
+                    T sg = (sine && (m & 1)) ? -s : s;
+                    stg[(2 * loc) * N + m] = x.x * sg;
+                    stg[(2 * loc + 1) * N + m] = x.y * sg;
+                };
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+                fence_proxy_async_smem();
+                __syncthreads();
+                if (tid == 0){
+                    long long lines = ((long long)TPB * 2 < P.G - c0) ? (long long)TPB * 2 : (P.G - c0);
+                    bulk_s2g(out + base_of_fast(Lo, c0), stg, (uint32_t)(lines * N * sizeof(T)));
+                    bulk_commit();
+                }
+            } else {
+                auto st = [&](int n, C x){
+                    int m = (2 * n < N) ? 2 * n : 2 * (N - 1 - n) + 1;
+                    T sg = (sine && (m & 1)) ? -s : s;
+                    if (va) out[oa + m * oes] = x.x * sg;
+                    if (vb) out[obb + m * oes] = x.y * sg;
+                };
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
+            }
         }
         __syncthreads();
     }

@@ -67,8 +67,8 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
             (a.G <= Lo.count || Lo.bstride == Lo.count * Lo.dist) && (obase & 15) == 0 &&
             (a.G % 2 == 0 || Lo.dist % 2 == 0))
             P.bulk_store = 1;
-        if (KIND == PK_C2R_BWD && N >= 32 && Lo.estride == 1 && Lo.dist == N &&
-            (a.G <= Lo.count || Lo.bstride == Lo.count * N) && (obase & 15) == 0)
+        if ((KIND == PK_C2R_BWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) && N >= 32 && Lo.estride == 1 &&
+            Lo.dist == N && (a.G <= Lo.count || Lo.bstride == Lo.count * N) && (obase & 15) == 0)
             P.bulk_store = 1;
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
