@@ -47,16 +47,32 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
     C *sm = reinterpret_cast<C*>(smraw);
     __shared__ long long s_tile;
     __shared__ int s_unit;
+    // first tile of every unit, for the tile -> unit search (shared memory
+    // when it fits, else the unit table itself)
+    constexpr int kUnitsInSmem = 1024;
+    __shared__ long long s_tile0[kUnitsInSmem];
     int tid = threadIdx.x;
+    bool const smem_units = nunits <= kUnitsInSmem;
+    if (smem_units)
+        for (int i = tid; i < nunits; i += blockDim.x) s_tile0[i] = units[i].tile0;
+    // the next tile is claimed while the current one is processed, so the
+    // queue atomic's latency is hidden; the smallest unfinished tile is
+    // always some CTA's current tile and depends only on smaller ones, so
+    // claiming ahead cannot stall the queue
+    long long next = 0;
+    if (tid == 0) next = (long long)atomicAdd(work_counter, 1ull);
+    __syncthreads();
     while (true){
         if (tid == 0){
-            s_tile = (long long)atomicAdd(work_counter, 1ull);
+            s_tile = next;
             int lo = 0, hi = nunits - 1;
             if (s_tile < total_tiles){
                 while (lo < hi){          // last unit with tile0 <= s_tile
                     int mid = (lo + hi + 1) >> 1;
-                    if (units[mid].tile0 <= s_tile) lo = mid; else hi = mid - 1;
+                    long long t0 = smem_units ? s_tile0[mid] : units[mid].tile0;
+                    if (t0 <= s_tile) lo = mid; else hi = mid - 1;
                 }
+                next = (long long)atomicAdd(work_counter, 1ull);
             }
             s_unit = lo;
         }
