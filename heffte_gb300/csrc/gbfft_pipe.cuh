@@ -108,7 +108,7 @@ struct PipeParams {
     int do_scale;
     int sine;
     int tswap;
-    int line_pitch;         // line tiles: input elements per line (LINE_LEN, or padded for c2r)
+    int line_pitch;         // line tiles: input elements per line (the line length, or padded for c2r)
     int bulk_store;         // c2c line tiles: results staged in the tile buffer, one bulk store per tile
     int *status;
 };
@@ -199,7 +199,6 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     constexpr int IN_ES = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) ? (int)sizeof(T) : (int)sizeof(C);
     constexpr int ROWS = (KIND == PK_C2R_BWD) ? H : N;
     constexpr int WIDTH = PAIRED ? 2 * TPB : TPB;           // input elements per tile row (columns)
-    constexpr int LINE_LEN = (KIND == PK_C2R_BWD) ? H : N;  // input elements per line
     constexpr bool FWD = (KIND == PK_C2C_FWD || KIND == PK_R2C_FWD || KIND == PK_R2R_FWD);
     constexpr int PADN = pipe_padn(N);
 
