@@ -66,6 +66,35 @@ def test_plan_rejects_unsupported_length(gb):
     assert e.value.code == 3 and "17" in str(e.value)
 
 
+def test_dct1_plans_and_scale(gb):
+    """rtransform<cos1>: lengths n >= 2 whose 2(n-1) factors into 2..13, scale
+    1/(64 prod(n_i - 1)) (include/heffte_fft3d.h:643-647)."""
+    b = gb.box3d((0, 0, 0), (32, 24, 16))           # 33 x 25 x 17: FFTs of 64, 48, 32
+    p = gb.rtransform(gb.kind.cos1, b, b)
+    assert p.size_inbox() == 33 * 25 * 17
+    assert p.get_scale_factor(gb.scale.full) == pytest.approx(1.0 / (64 * 32 * 24 * 16))
+    for bad in ((31, 7, 7), (0, 7, 7)):                # 2 * 31 = 62 has the factor 31; n = 1
+        with pytest.raises(gb.HeffteError) as e:
+            bb = gb.box3d((0, 0, 0), bad)
+            gb.rtransform(gb.kind.cos1, bb, bb)
+        assert e.value.code == 3 and "DCT-I" in str(e.value)
+
+
+def test_plan_option_setters_validate(gb):
+    b = gb.box3d((0, 0, 0), (63, 31, 15))
+    p = gb.fft3d(b, b)
+    p.set_tensor_cores(True)
+    p.set_tensor_cores(False)
+    p.set_knobs(1, 2, 1)
+    p.set_knobs(0, 1, 0)
+    L = gb.lib()
+    assert L.heffte_gb300_plan_set_tensor_cores(p._h, 2) == 1
+    for args in ((2, 1, 0), (0, 3, 0), (0, 1, 2), (-1, 1, 0)):
+        assert L.heffte_gb300_plan_set_knobs(p._h, *args) == 1
+    assert L.heffte_gb300_plan_set_tensor_cores(None, 1) == 1
+    assert p.size_inbox() == 64 * 32 * 16          # the plan survives rejected settings
+
+
 def test_raw_abi_status_codes(gb):
     L = gb.lib()
     h = ctypes.c_void_p()
