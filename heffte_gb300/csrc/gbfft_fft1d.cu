@@ -3,6 +3,7 @@
 #include "gbfft_internal.h"
 #include "gbfft_pipe.cuh"
 #include <atomic>
+#include <cstring>
 #include <map>
 #include <math.h>
 
@@ -337,6 +338,76 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
     return launch_pipe_f64_r2r(s, kind, f.N, cols, a);
 }
 
+// Pipelined runtime-radix path (c2c of any supported length): line tiles need
+// back-to-back lines whose tile bytes are multiples of 16, column tiles a
+// tensor map over adjacent columns.  Returns false when the batch does not
+// fit either form (the generic kernels run it then).
+static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
+                        long long G, double scale, LaunchCfg const &cfg){
+    int v = (cfg.variant != 0) ? cfg.variant : kernel_variant();
+    if (v == 1 || f.N < 8 || f.plan.nstages < 1) return false;
+    bool same = Li.count == Lo.count && Li.dist == Lo.dist && Li.bstride == Lo.bstride && Li.estride == Lo.estride;
+    if (in == out && !same) return false;
+    bool cols = !(Li.estride == 1 && Lo.estride == 1);
+    if (!cols && Li.estride != 1) return false;
+    merge_blocks(Li, Lo, G);
+    int N = f.N, T = f.plan.T;
+    size_t es = (prec == 0) ? sizeof(float2) : sizeof(double2);
+    size_t padn = (size_t)(N + N / 16 + 1);
+    uintptr_t base = reinterpret_cast<uintptr_t>(in);
+    if (base & 15) return false;
+    PipeRtParams P{};
+    CUtensorMap tmap;
+    std::memset(&tmap, 0, sizeof(tmap));
+    int tpb;
+    size_t smem;
+    if (!cols){
+        if (Li.dist != N || (G > Li.count && Li.bstride != Li.count * N)) return false;
+        tpb = std::max(1, 256 / T);
+        while (tpb > 1 && tpb * T > 512) tpb /= 2;
+        while (tpb > 1 && (2 * (size_t)tpb * N + (size_t)tpb * padn) * es > 200 * 1024) tpb /= 2;
+        smem = (2 * (size_t)tpb * N + (size_t)tpb * padn) * es;
+        long long last = G % tpb;
+        if (((size_t)tpb * N * es) % 16 != 0 || ((size_t)last * N * es) % 16 != 0) return false;
+        P.ntiles = (G + tpb - 1) / tpb;
+        P.tiles_per_block = 0;
+    } else {
+        if (Li.dist != 1 || G % Li.count != 0) return false;
+        tpb = (prec == 0) ? 16 : 8;
+        while (tpb > 2 && tpb * T > 512) tpb /= 2;
+        while (tpb > 2 && 2 * (size_t)tpb * N * es > 200 * 1024) tpb /= 2;
+        if (((size_t)tpb * es) % 16 != 0 || tpb * T > 512) return false;
+        smem = 2 * (size_t)tpb * N * es;
+        // the rows of each tensor copy: a divisor of N up to 256 whose box
+        // (and so every box destination) is a multiple of 128 bytes, as is
+        // the tile buffer, since a tensor copy's shared-memory destination
+        // must be 128-byte aligned
+        int boxr = 0;
+        for (int d = std::min(N, 256); d >= 1; d--)
+            if (N % d == 0 && ((size_t)d * tpb * es) % 128 == 0){ boxr = d; break; }
+        if (boxr == 0 || ((size_t)tpb * N * es) % 128 != 0) return false;
+        long long blocks = G / Li.count;
+        int swap = 0;
+        if (!encode_column_tmap(&tmap, in, (int)es, Li.count, N, blocks, Li.estride, Li.bstride, tpb, boxr, &swap))
+            return false;
+        P.boxr = boxr;
+        P.tswap = swap;
+        P.tiles_per_block = (Li.count + tpb - 1) / tpb;
+        P.ntiles = blocks * P.tiles_per_block;
+    }
+    if (smem > 226 * 1024) return false;
+    P.plan = f.plan;
+    P.Li = Li; P.Lo = Lo; P.in = in; P.out = out;
+    P.tw = f.twiddles(prec, s);
+    P.G = G;
+    P.tpb = tpb;
+    P.scale = scale;
+    P.do_scale = (scale != 1.0);
+    P.status = device_status();
+    launch_pipe_rt(s, prec, fwd, cols, P, &tmap, smem, tpb * T);
+    return true;
+}
+
 void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
@@ -345,6 +416,7 @@ void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout 
         return;
     }
     if (try_pipe(s, fwd ? K_C2C_F : K_C2C_B, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
+    if (try_pipe_rt(s, f, prec, fwd, Li, Lo, in, out, G, scale, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, false, G, cfg, a);

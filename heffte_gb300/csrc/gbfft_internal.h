@@ -130,6 +130,27 @@ struct PipeLaunch {
     int sine;
     int *status;
 };
+// Pipelined complex transforms of any supported length (runtime radix plan,
+// gbfft_pipe_rt.cuh): the parameters of one launch and its dispatcher.
+struct PipeRtParams {
+    Plan1D plan;
+    Layout Li, Lo;
+    void const *in;
+    void *out;
+    void const *tw;
+    long long G;
+    long long ntiles;
+    long long tiles_per_block;   // column tiles covering one block of `count` columns
+    int tpb;                     // transforms per tile
+    int boxr;                    // rows per tensor-map copy (divides N)
+    int tswap;
+    double scale;
+    int do_scale;
+    int *status;
+};
+void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
+                    size_t smem, int threads);
+
 // one dispatcher per precision and kind group (c2c / r2c+c2r / r2r), kind = K_*
 bool launch_pipe_f32_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 bool launch_pipe_f32_r2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);

@@ -1,0 +1,141 @@
+// Pipelined complex transforms of any supported length (runtime radix plan):
+// the persistent, double-buffered tile pipeline of the power-of-two kernels
+// (lines by 1-D bulk copies, columns by 3-D tensor-map copies, both
+// completing on mbarriers with bounded waits) around the runtime Stockham
+// stages of the generic kernels (radices 2, 3, 4, 5, 7, 8, 11, 13, 16).
+//
+//   * line tiles: TPB whole lines land in shared memory unpadded; stage 0
+//     reads them there and the later stages exchange through a padded
+//     buffer; the last stage stores to global memory;
+//   * column tiles: TPB adjacent columns land as a [row][column] tile, which
+//     is the stages' exchange layout, so every stage (stage 0 included) runs
+//     in place in the tile.
+// While a tile is transformed the next one is already being copied in.
+#pragma once
+#include <cuda.h>
+#include "gbfft_kernels.cuh"
+#include "gbfft_ptx.cuh"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+enum { RT_LD_BULK = 0, RT_LD_TENSOR = 1 };
+
+// All stages of one tile; sm_x: exchange buffer (line tiles), or the tile
+// itself (column tiles).
+template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+__device__ __forceinline__ void rt_stages(Plan1D const &P, int t, bool active, c_t<T> *sm_x, int loc, int TPB,
+                                          int padn, c_t<T> const *__restrict__ tw, LD &ld, ST &st){
+    Regs<T, EMAX> r;
+    for (int s = 0; s < P.nstages; s++){
+        Stage const S = P.st[s];
+        // line tiles read stage 0 from the unpadded tile (ld); column tiles
+        // read every stage from the tile in place (read, barrier, write)
+        bool first = !COLS && (s == 0);
+        bool tg = (s == P.nstages - 1);
+        switch (S.R){
+            case 16: if constexpr (EMAX >= 16) fft_stage<16, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 13: if constexpr (EMAX >= 13) fft_stage<13, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 11: if constexpr (EMAX >= 11) fft_stage<11, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 8: fft_stage<8, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 7: fft_stage<7, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 5: fft_stage<5, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 4: fft_stage<4, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            case 3: fft_stage<3, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+            default: fft_stage<2, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm_x, loc, TPB, padn, tw, r, ld, st); break;
+        }
+    }
+}
+
+template<typename T, bool FWD, bool COLS, int LOADER>
+__global__ void __launch_bounds__(512)
+k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtensorMap tmap){
+    using C = c_t<T>;
+    constexpr int EMAX = kEmax;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __shared__ __align__(8) uint64_t bar[2];
+    int const N = P.plan.N, TPB = P.tpb;
+    int const padn = padded_len(N);
+    long long const TILE = (long long)TPB * N;             // complex values per tile buffer
+    C *tiles = reinterpret_cast<C*>(smraw);
+    C *xline = tiles + 2 * TILE;                           // line tiles: padded exchange buffer
+    int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int loc, t;
+    thread_map<COLS>(TPB, P.plan.T, loc, t);
+    Layout const Li = P.Li, Lo = P.Lo;
+
+    if (tid == 0){
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        if (LOADER == RT_LD_TENSOR) prefetch_tmap(&tmap);
+    }
+    __syncthreads();
+
+    auto tile_origin = [&](long long tile, long long &blk, long long &c0){
+        if (COLS){ blk = tile / P.tiles_per_block; c0 = (tile - blk * P.tiles_per_block) * TPB; }
+        else { blk = 0; c0 = tile * (long long)TPB; }
+    };
+    auto issue = [&](long long tile, int b){
+        if (warp != 0 || lane != 0) return;
+        long long blk, c0;
+        tile_origin(tile, blk, c0);
+        unsigned char *dst = reinterpret_cast<unsigned char*>(tiles + b * TILE);
+        if constexpr (LOADER == RT_LD_TENSOR){
+            constexpr int WPE = (sizeof(C) >= 8) ? (int)sizeof(C) / 8 : 1;
+            mbar_arrive_expect_tx(&bar[b], (uint32_t)((long long)N * TPB * sizeof(C)));
+            int x = (int)(c0 * WPE);
+            for (int r0 = 0; r0 < N; r0 += P.boxr){
+                unsigned char *d = dst + (size_t)r0 * TPB * sizeof(C);
+                if (P.tswap) tma_load_3d(d, &tmap, x, (int)blk, r0, &bar[b]);
+                else tma_load_3d(d, &tmap, x, r0, (int)blk, &bar[b]);
+            }
+        } else {
+            long long lines = ((long long)TPB < P.G - c0) ? (long long)TPB : (P.G - c0);
+            uint32_t bytes = (uint32_t)(lines * N * sizeof(C));
+            mbar_arrive_expect_tx(&bar[b], bytes);
+            bulk_g2s(dst, reinterpret_cast<C const*>(P.in) + base_of(Li, c0), bytes, &bar[b]);
+        }
+    };
+
+    uint32_t ph0 = 0, ph1 = 0;
+    long long tile = blockIdx.x;
+    if (tile < P.ntiles) issue(tile, 0);
+    T const sc = (T)P.scale;
+    C const *tw = reinterpret_cast<C const*>(P.tw);
+    for (int it = 0; tile < P.ntiles; tile += gridDim.x, it++){
+        int b = it & 1;
+        long long nxt = tile + gridDim.x;
+        if (nxt < P.ntiles){
+            if (warp == 0) fence_proxy_async_smem();
+            issue(nxt, b ^ 1);
+        }
+        bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0, P.status);
+        if (__syncthreads_or(!ok)) return;
+        if (b) ph1 ^= 1; else ph0 ^= 1;
+
+        C *tb = tiles + b * TILE;
+        long long blk, c0;
+        tile_origin(tile, blk, c0);
+        bool active, valid;
+        long long oa = 0;
+        if (COLS){
+            long long ca = c0 + loc;
+            valid = ca < Li.count;
+            oa = blk * Lo.bstride + ca * Lo.dist;
+        } else {
+            long long g = c0 + loc;
+            valid = g < P.G;
+            if (valid) oa = base_of(Lo, g);
+        }
+        active = valid && (t < P.plan.T) && (loc < TPB);
+        C *out = reinterpret_cast<C*>(P.out);
+        long long const oes = Lo.estride;
+        auto ld = [&](int p) -> C { return tb[(long long)loc * N + p]; };
+        auto st = [&](int p, C x){ out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
+        rt_stages<EMAX, FWD, COLS, T>(P.plan, t, active, COLS ? tb : xline, loc, TPB, padn, tw, ld, st);
+        __syncthreads();
+    }
+}
+
+} // namespace gbfft
