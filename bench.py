@@ -451,6 +451,12 @@ WORKLOADS = {
     "batch256loop": ("batch", "loop", 0),
     # learned plan selection on the 2000 measured shapes (tests/golden/selector_timings.npz)
     "selector2000": ("selector", None, 0),
+    # the step of the reference's convolution benchmark on 512^3 complex<float>
+    # (in place: forward, X .* X, backward) through plan.convolve; fused route,
+    # the unfused route (the reference's order of operations), and two inputs
+    "conv512": ("conv", (512, 512, 512), 0, "self"),
+    "conv512unfused": ("conv", (512, 512, 512), 0, "self-unfused"),
+    "conv512xy": ("conv", (512, 512, 512), 0, "xy"),
 }
 
 BATCH_SIDES = [16, 24, 32, 40, 48, 64, 80, 96, 128]
@@ -584,12 +590,79 @@ def run_selector_workload(name):
             "dataset_device": str(d["device"])}
 
 
+def run_conv_workload(name, steps, warmup):
+    """plan.convolve on a c2c box: time per convolution, GFLOP/s counting
+    its transforms (5 N log2 N each: 2 for x .* x, 3 for x .* y), the bytes of
+    its passes against the HBM peak, and the result against this library's
+    complex<double> convolution of the same input (the FP64 path the parity
+    tests hold to 1e-12 of the FP64 oracle)."""
+    import torch
+    import heffte_gb300 as gb
+    _, size, prec, form = WORKLOADS[name]
+    N = size[0] * size[1] * size[2]
+    stream = torch.cuda.current_stream()
+    box = gb.box3d((0, 0, 0), [s - 1 for s in size])
+    plan = gb.fft3d(box, box, stream=stream)
+    if form == "self-unfused":
+        plan.set_convolution_fusion(False)
+    two = form == "xy"
+    rdt = torch.float32 if prec == 0 else torch.float64
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(99)
+
+    def rand():
+        return torch.complex(torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1,
+                             torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1)
+    x = rand()
+    y = rand() if two else None
+    # out of place: the benchmark's in-place loop feeds each result back in,
+    # which under- or overflows after a few steps; the passes are the same
+    out = torch.empty_like(x)
+    work = torch.empty(plan.convolve_workspace(), dtype=x.dtype, device="cuda")
+    route = plan.convolve_route(prec, two)
+
+    def step():
+        plan.convolve(x, y, out, gb.scale.full, workspace=work)
+
+    for _ in range(warmup):
+        step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ntrans = 3 if two else 2
+    cs = 8 if prec == 0 else 16
+    # passes over the box in units of N complex values moved (read or write):
+    # fused self 5 passes (10); fused xy 2 + 2 forward passes, the fused pass
+    # (2 reads, 1 write), 2 backward passes (15); unfused self 3 + 3 transform
+    # passes and the product's read + write (14; 18 with y's forward and read)
+    units = (15 if two else 10) if route >= 0 else (18 if two else 14)
+    b = units * N * cs
+    peak, _ = peaks()
+    del work
+    x64 = x.to(torch.complex128)
+    y64 = y.to(torch.complex128) if two else None
+    o64 = torch.empty_like(x64)
+    gb.fft3d(box, box, stream=stream).convolve(x64, y64, o64, gb.scale.full)
+    err = float((torch.linalg.vector_norm(out.to(torch.complex128) - o64) / torch.linalg.vector_norm(o64)).item())
+    return {"workload": name, "form": form, "fused_dim": route, "ms_per_step": ms,
+            "gflops": ntrans * flops_per_transform(N) / (ms / 1e3) / 1e9,
+            "pass_units": units, "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak,
+            "rel_l2_vs_fp64": err}
+
+
 def run_workload(name, steps, warmup):
     import torch
     import heffte_gb300 as gb
     kind, size, prec = WORKLOADS[name][:3]
     if kind == "selector":
         return run_selector_workload(name)
+    if kind == "conv":
+        return run_conv_workload(name, steps, warmup)
     tc = len(WORKLOADS[name]) > 3 and WORKLOADS[name][3]
     if kind == "batch":
         cache = "loop" if size == "loop" else None

@@ -76,6 +76,11 @@ def lib():
     L.heffte_gb300_scale_factor.restype = d
     L.heffte_gb300_forward.argtypes = [vp, i, vp, vp, vp, i]
     L.heffte_gb300_backward.argtypes = [vp, i, vp, vp, vp, i]
+    L.heffte_gb300_convolve_workspace.argtypes = [vp]
+    L.heffte_gb300_convolve_workspace.restype = ll
+    L.heffte_gb300_convolve.argtypes = [vp, i, vp, vp, vp, vp, i]
+    L.heffte_gb300_convolve_route.argtypes = [vp, i, i, ctypes.POINTER(ctypes.c_int)]
+    L.heffte_gb300_plan_set_convolution_fusion.argtypes = [vp, i]
     L.heffte_gb300_forward_batch.argtypes = [vp, i, i, vp, vp, vp, i]
     L.heffte_gb300_backward_batch.argtypes = [vp, i, i, vp, vp, vp, i]
     L.heffte_gb300_boxbatch_create.argtypes = [i, i, i, ctypes.POINTER(ctypes.c_int), vp, ctypes.POINTER(vp)]
@@ -277,6 +282,39 @@ class _plan:
 
     def backward_buffered(self, inarray, outarray, workspace, scaling=scale.none):
         self._run(False, inarray, outarray, workspace, scaling)
+
+    def convolve_workspace(self):
+        return lib().heffte_gb300_convolve_workspace(self._h)
+
+    def set_convolution_fusion(self, enable=True):
+        """convolve's fused route where it applies (default), or always the unfused sequence."""
+        check(lib().heffte_gb300_plan_set_convolution_fusion(self._h, 1 if enable else 0))
+
+    def convolve_route(self, precision=0, two_inputs=False):
+        """Dimension of the fused convolution pass for aligned arrays, -1 when unfused."""
+        d = ctypes.c_int(-2)
+        check(lib().heffte_gb300_convolve_route(self._h, precision, 1 if two_inputs else 0, ctypes.byref(d)))
+        return d.value
+
+    def convolve(self, x, y, outarray, scaling=scale.full, workspace=None):
+        """outarray = backward(forward(x) .* forward(y)) with the backward scaling
+        (scale.full: the circular convolution of x and y); y None: x .* x.
+        The step of the reference's benchmarks/convolution.cpp as one call."""
+        if scaling not in (0, 1, 2):
+            raise heffte_input_error("called with invalid scaling")
+        if self.kind not in (kind.c2c, kind.r2c):
+            raise heffte_input_error("convolution needs a c2c or r2c plan")
+        n = self.size_inbox()
+        if x.numel() < n or outarray.numel() < n or (y is not None and y.numel() < n):
+            raise heffte_input_error("called with invalid array size")
+        if y is not None and y.dtype != x.dtype:
+            raise heffte_input_error("x and y must have the same type")
+        it, ot = str(x.dtype), str(outarray.dtype)
+        table = _CPLX if self.kind == kind.c2c else _REAL
+        if it not in table or it != ot:
+            raise heffte_input_error("convolution arrays must have the plan's input type")
+        check(lib().heffte_gb300_convolve(self._h, table[it], _ptr(x), _ptr(y), _ptr(outarray), _ptr(workspace),
+                                          scaling))
 
     def forward_batch(self, batch, inarray, outarray, scaling=scale.none, workspace=None):
         self._run(True, inarray, outarray, workspace, scaling, batch)

@@ -276,6 +276,27 @@ int heffte_gb300_backward_batch(heffte_gb300_plan plan, int batch, int prec, con
     return exec(plan, false, batch, prec, input, output, workspace, scale);
 }
 
+long long heffte_gb300_convolve_workspace(heffte_gb300_plan plan){ return plan ? plan->p->convolve_workspace() : -1; }
+
+int heffte_gb300_convolve_route(heffte_gb300_plan plan, int prec, int two_inputs, int *fused_dim){
+    return guard([&]{
+        if (!plan || !fused_dim) throw Error(ST_INVALID, "null plan or result pointer");
+        if (prec != 0 && prec != 1) throw Error(ST_INVALID, "precision must be 0 (single) or 1 (double)");
+        // 256-byte aligned stand-ins: the check only looks at the alignment
+        void *aligned = reinterpret_cast<void*>((uintptr_t)1 << 20);
+        *fused_dim = plan->p->convolve_fused_dim(prec, aligned, two_inputs ? aligned : nullptr);
+    });
+}
+
+int heffte_gb300_convolve(heffte_gb300_plan plan, int prec, const void *x, const void *y, void *output,
+                          void *workspace, int scale){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan");
+        plan->p->convolve(prec, x, y, output, workspace, scale);
+        check_cuda(cudaPeekAtLastError(), "convolution");
+    });
+}
+
 // ---------------------------------------------------------------------------
 // batches of uneven boxes, autotuner
 // ---------------------------------------------------------------------------
@@ -367,6 +388,14 @@ int heffte_gb300_plan_set_tensor_cores(heffte_gb300_plan plan, int enable){
         Knobs k = p.knobs;
         k.tensor_cores = enable;
         plan->p = make_plan(p.kind, p.inbox, p.outbox, p.r2c_dir, p.opts, p.stream, k);
+    });
+}
+
+int heffte_gb300_plan_set_convolution_fusion(heffte_gb300_plan plan, int enable){
+    return guard([&]{
+        if (!plan) throw Error(ST_INVALID, "null plan");
+        if (enable != 0 && enable != 1) throw Error(ST_INVALID, "enable must be 0 or 1");
+        plan->p->knobs.conv_fused = enable;
     });
 }
 

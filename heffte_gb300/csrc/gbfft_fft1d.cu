@@ -426,6 +426,23 @@ void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout 
     run(s, fwd ? K_C2C_F : K_C2C_B, prec, cols, a);
 }
 
+// Fused convolution pass over the columns of x (in place): power-of-two
+// lengths of the pipelined radix plan, column layouts (estride != 1) whose
+// tiles a tensor map can copy.  Returns false when the pass cannot run.
+bool launch_conv_pass(cudaStream_t s, Fft1D &f, int prec, Layout L, void *x, void const *y, long long G,
+                      double scale, bool dry_run){
+    if (kernel_variant() == 1) return false;
+    std::vector<int> pr = pipe_radices(f.N);
+    if (pr.empty() || pr != f.radices || f.N < 16 || L.estride == 1) return false;
+    Layout Lo = L;
+    merge_blocks(L, Lo, G);
+    ConvLaunch a{};
+    a.L = L; a.x = x; a.y = y; a.G = G; a.scale = scale;
+    a.status = device_status();
+    a.tw = dry_run ? nullptr : f.twiddles(prec, s);
+    return (prec == 0) ? launch_conv_f32(s, f.N, a, dry_run) : launch_conv_f64(s, f.N, a, dry_run);
+}
+
 void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;

@@ -158,6 +158,25 @@ bool launch_pipe_f32_r2r(cudaStream_t s, int kind, int N, bool cols, PipeLaunch 
 bool launch_pipe_f64_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 bool launch_pipe_f64_r2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 bool launch_pipe_f64_r2r(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+// Fused convolution pass (gbfft_conv.cuh): forward FFT of the columns of x
+// (and y), pointwise product, scale, backward FFT, in place in x.
+struct ConvLaunch {
+    Layout L;
+    void *x;
+    void const *y;     // null: self-convolution (X .* X)
+    void const *tw;
+    long long G;
+    double scale;
+    int *status;
+};
+// dry_run: only checks that the pass can run (length, alignment, tensor maps)
+bool launch_conv_f32(cudaStream_t s, int N, ConvLaunch const &a, bool dry_run);
+bool launch_conv_f64(cudaStream_t s, int N, ConvLaunch const &a, bool dry_run);
+bool launch_conv_pass(cudaStream_t s, Fft1D &f, int prec, Layout L, void *x, void const *y, long long G,
+                      double scale, bool dry_run);
+// a[i] = a[i] * b[i] * scale (b null: a[i]^2 * scale) over n complex values
+void launch_pointwise(cudaStream_t s, int prec, long long n, void *a, void const *b, double scale);
+
 // Tensor map over a batch of column transforms: x = column (8-byte words),
 // then rows and blocks ordered by ascending stride (*swap = 1 when blocks
 // come before rows).  Returns false if the driver rejects the geometry.

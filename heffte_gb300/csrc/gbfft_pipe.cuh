@@ -114,13 +114,16 @@ struct PipeParams {
 };
 
 // One radix stage; S == 0 reads through ld0, the last stage writes through st
-// (or to the exchange buffer when POST is set).
-template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST, class LD, class ST>
+// (or to the exchange buffer when POST is set).  Stages S .. SEND-1 run
+// (SEND below the stage count stops early, the last run stage writing the
+// exchange buffer).
+template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST, int SEND = pipe_nstages(N), class LD,
+         class ST>
 __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const *__restrict__ tw,
                                        c_t<T> (&v)[16], LD &ld0, ST &st){
     using C = c_t<T>;
     constexpr int NS = pipe_nstages(N);
-    if constexpr (S < NS){
+    if constexpr (S < SEND){
         constexpr int R = pipe_radix(N, S), Ns = pipe_ns(N, S), TWO = pipe_twoff(N, S);
         constexpr int NR = N / R, TT = pipe_tt(N), M = pipe_pe(N) / R, PADN = pipe_padn(N);
         constexpr bool LAST = (S == NS - 1);
@@ -161,7 +164,7 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
             }
         }
         if (TO_XCH) __syncthreads();
-        pstage<T, N, TPB, S + 1, FWD, COLS, POST>(t, loc, xch, tw, v, ld0, st);
+        pstage<T, N, TPB, S + 1, FWD, COLS, POST, SEND>(t, loc, xch, tw, v, ld0, st);
     }
 }
 

@@ -330,6 +330,7 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
 
 Plan3D::~Plan3D(){
     if (cached_work) cudaFree(cached_work);
+    if (conv_cache) cudaFree(conv_cache);
 }
 
 double Plan3D::get_scale(int scaling) const{
@@ -425,6 +426,89 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// convolution (benchmarks/convolution.cpp: forward, pointwise product, backward)
+// ---------------------------------------------------------------------------
+// Fused route (c2c, no reshapes, the same order on both sides): the forward
+// passes along two dimensions, then ONE pass along the third that transforms
+// each column forward, multiplies it by y's column (or squares it), scales and
+// transforms it back (gbfft_conv.cuh), then the backward passes along the two
+// other dimensions.  Five passes over the box for a self-convolution where
+// the unfused sequence makes six transform passes and a product pass.
+int Plan3D::convolve_fused_dim(int prec, void *out, void const *wy) const{
+    if (kind != PK_C2C || opts.use_reorder || inbox.order != outbox.order) return -1;
+    if (!knobs.conv_fused || knobs.tensor_cores || knobs.variant == 1 || knobs.radix_policy != 0) return -1;
+    Box3 const &B = inbox;
+    for (int d = 0; d < 3; d++) if (B.size[d] < 2) return -1;
+    for (int fi : {2, 1}){
+        int f = B.order[fi];
+        auto ff = get_fft1d((int)B.size[f]);
+        if (launch_conv_pass(stream, *ff, prec, pass_layout(B, f, B.order), out, wy, B.count() / B.size[f], 1.0, true))
+            return f;
+    }
+    return -1;
+}
+
+bool Plan3D::convolve_fused(int prec, void const *x, void const *y, void *out, void *wy, double scale){
+    int f = convolve_fused_dim(prec, out, y ? wy : nullptr);
+    if (f < 0) return false;
+    Box3 const &B = inbox;
+    std::array<int, 3> const io = B.order;
+    LaunchCfg cfg;
+    {
+        int rest[2], k = 0;
+        for (int i = 0; i < 3; i++) if (io[i] != f) rest[k++] = io[i];
+        auto ff = get_fft1d((int)B.size[f]);
+        Layout Lf = pass_layout(B, f, io);
+        long long Gf = B.count() / B.size[f];
+        auto f0 = get_fft1d((int)B.size[rest[0]]), f1 = get_fft1d((int)B.size[rest[1]]);
+        Layout L0 = pass_layout(B, rest[0], io), L1 = pass_layout(B, rest[1], io);
+        long long G0 = B.count() / B.size[rest[0]], G1 = B.count() / B.size[rest[1]];
+        // y first: y may alias out
+        if (y){
+            launch_c2c(stream, *f0, prec, true, L0, L0, y, wy, G0, 1.0, cfg);
+            launch_c2c(stream, *f1, prec, true, L1, L1, wy, wy, G1, 1.0, cfg);
+        }
+        launch_c2c(stream, *f0, prec, true, L0, L0, x, out, G0, 1.0, cfg);
+        launch_c2c(stream, *f1, prec, true, L1, L1, out, out, G1, 1.0, cfg);
+        if (!launch_conv_pass(stream, *ff, prec, Lf, out, y ? wy : nullptr, Gf, scale, false))
+            throw Error(ST_CUDA, "fused convolution pass refused after its check passed");
+        launch_c2c(stream, *f1, prec, false, L1, L1, out, out, G1, 1.0, cfg);
+        launch_c2c(stream, *f0, prec, false, L0, L0, out, out, G0, 1.0, cfg);
+    }
+    return true;
+}
+
+void Plan3D::convolve(int prec, void const *x, void const *y, void *out, void *work, int scaling){
+    if (prec != 0 && prec != 1) throw Error(ST_INVALID, "precision must be 0 (single) or 1 (double)");
+    if (scaling < 0 || scaling > 2) throw Error(ST_INVALID, "invalid scaling");
+    if (!x || !out) throw Error(ST_INVALID, "null input or output pointer");
+    if (kind != PK_C2C && kind != PK_R2C) throw Error(ST_UNSUPPORTED, "convolution needs a c2c or r2c plan");
+    bool self = (y == nullptr || y == x);
+    size_t ces = (prec == 0) ? 8 : 16;
+    size_t need = (size_t)convolve_workspace() * ces;
+    char *w = static_cast<char*>(work);
+    if (!w){
+        if (conv_cache_bytes < need){
+            if (conv_cache) check_cuda(cudaFree(conv_cache), "cudaFree(convolution workspace)");
+            conv_cache = nullptr;
+            conv_cache_bytes = 0;
+            check_cuda(cudaMalloc(&conv_cache, need), "cudaMalloc(convolution workspace)");
+            conv_cache_bytes = need;
+        }
+        w = static_cast<char*>(conv_cache);
+    }
+    char *w1 = w + (size_t)work_elems * ces;          // spectrum of x
+    char *w2 = w1 + (size_t)size_outbox() * ces;      // spectrum of y
+    if (convolve_fused(prec, x, self ? nullptr : y, out, w1, get_scale(scaling))) return;
+    // unfused: both forward transforms, the product kernel, the backward
+    // transform carrying the scale
+    if (!self) execute(true, prec, 1, y, w2, w, 0);
+    execute(true, prec, 1, x, w1, w, 0);
+    launch_pointwise(stream, prec, size_outbox(), w1, self ? nullptr : w2, 1.0);
+    execute(false, prec, 1, w1, out, w, scaling);
 }
 
 } // namespace gbfft

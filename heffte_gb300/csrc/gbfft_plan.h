@@ -80,12 +80,14 @@ enum PlanKind { PK_C2C = 0, PK_R2C = 1, PK_COS = 2, PK_SIN = 3, PK_COS1 = 4 };
 // family (0 pipelined where it applies, 1 generic only), tile of the generic
 // kernels (automatic / tile_div), radix order (0 default, 1 ascending); and
 // the precision form of the complex<float> passes (tensor_cores = 1: radix-16
-// stages as split-BF16 DFT contractions on the tensor cores).
+// stages as split-BF16 DFT contractions on the tensor cores); whether
+// convolve may fuse its middle pass (conv_fused).
 struct Knobs {
     int variant = 0;
     int tile_div = 1;
     int radix_policy = 0;
     int tensor_cores = 0;
+    int conv_fused = 1;
 };
 std::shared_ptr<Fft1D> fft_for(int N, int radix_policy);
 
@@ -114,6 +116,8 @@ struct Plan3D {
     double scale_factor = 1.0;    // "full" factor
     void *cached_work = nullptr;  // lazily allocated when the caller passes no workspace
     size_t cached_bytes = 0;
+    void *conv_cache = nullptr;   // the same for convolve()
+    size_t conv_cache_bytes = 0;
     Knobs knobs;
     ~Plan3D();
 
@@ -122,6 +126,16 @@ struct Plan3D {
     long long size_workspace() const { return work_elems; }
     double get_scale(int scaling) const;
     void execute(bool forward, int prec, int batch, void const *in, void *out, void *work, int scaling);
+    // Circular convolution through the plan's transforms (benchmarks/convolution.cpp):
+    // out = backward(forward(x) .* forward(y)) with the backward scaling;
+    // y null or equal to x: self-convolution.  Workspace in complex elements.
+    long long convolve_workspace() const { return work_elems + 2 * size_outbox(); }
+    void convolve(int prec, void const *x, void const *y, void *out, void *work, int scaling);
+    // the fused route of convolve for c2c plans; false when it does not apply
+    bool convolve_fused(int prec, void const *x, void const *y, void *out, void *wy, double scale);
+    // the dimension the fused route transforms in its fused pass (-1: unfused);
+    // only the alignment of out and wy (null: self-convolution) is looked at
+    int convolve_fused_dim(int prec, void *out, void const *wy) const;
 };
 
 std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbox, int r2c_dir, Options const &o,

@@ -9,6 +9,7 @@
 //   step 1 post_forward: complex H   -> real N   (Re X_k, or -Im X_{k+1} for sin)
 //   step 2 pre_backward: real N      -> complex H
 //   step 3 post_backward: real M     -> real N   (odd entries, even entries for cos1)
+// Also the pointwise spectrum product of the unfused convolution path.
 #include "gbfft_internal.h"
 
 namespace gbfft {
@@ -71,6 +72,35 @@ void launch_prepost(cudaStream_t s, int prec, int kind, int step, int N, long lo
     long long blocks = std::min<long long>((total + 255) / 256, (long long)num_sms() * 32);
     if (prec == 0) k_prepost<float><<<(unsigned)blocks, 256, 0, s>>>(kind, step, N, lines, in_ld, out_ld, out_len, in, out);
     else k_prepost<double><<<(unsigned)blocks, 256, 0, s>>>(kind, step, N, lines, in_ld, out_ld, out_len, in, out);
+}
+
+} // namespace gbfft
+
+namespace gbfft {
+
+// Pointwise product of two spectra (the middle step of benchmarks/convolution.cpp,
+// output_array[i] *= output_array[i] there), scaled: a[i] = a[i] * b[i] * s,
+// or a[i]^2 * s when b is null.  Grid-stride over n complex values.
+template<typename T>
+__global__ void __launch_bounds__(256)
+k_pointwise(long long n, c_t<T> *a, c_t<T> const *b, T s){
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x){
+        c_t<T> u = a[i];
+        c_t<T> v = b ? b[i] : u;
+        a[i] = cscale(cmul(u, v), s);
+    }
+}
+
+void launch_pointwise(cudaStream_t s, int prec, long long n, void *a, void const *b, double scale){
+    if (n <= 0) return;
+    long long blocks = std::min<long long>((n + 255) / 256, (long long)num_sms() * 16);
+    if (prec == 0)
+        k_pointwise<float><<<(unsigned)blocks, 256, 0, s>>>(n, static_cast<float2*>(a), static_cast<float2 const*>(b),
+                                                           (float)scale);
+    else
+        k_pointwise<double><<<(unsigned)blocks, 256, 0, s>>>(n, static_cast<double2*>(a),
+                                                             static_cast<double2 const*>(b), scale);
+    check_cuda(cudaPeekAtLastError(), "pointwise product launch");
 }
 
 } // namespace gbfft

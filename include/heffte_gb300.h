@@ -228,6 +228,27 @@ int heffte_gb300_forward_batch(heffte_gb300_plan plan, int batch, int prec, cons
 int heffte_gb300_backward_batch(heffte_gb300_plan plan, int batch, int prec, const void *input, void *output,
                                 void *workspace, int scale);
 
+/* Circular convolution through the plan's transforms, the step of the
+ * reference's convolution benchmark (benchmarks/convolution.cpp:89-95:
+ * forward, pointwise product, backward) as one call:
+ *     output = backward( forward(x) .* forward(y) ),
+ * both forward transforms unscaled, the backward one scaled by `scale`
+ * (HEFFTE_GB300_SCALE_FULL gives the circular convolution of x and y).
+ * y = NULL or y = x: self-convolution (the benchmark's X .* X).  c2c plans
+ * take and return complex inbox arrays, r2c plans real ones (the product
+ * runs on the half spectrum).  x, y and output may alias one another.
+ * workspace = NULL uses a buffer the plan allocates once, else it holds
+ * convolve_workspace() complex elements.  On c2c plans without reshapes the
+ * forward transform along one dimension, the product and the backward
+ * transform along it run as one fused kernel. */
+long long heffte_gb300_convolve_workspace(heffte_gb300_plan plan);
+/* The route convolve takes for 16-byte aligned arrays: *fused_dim = the
+ * dimension of the fused pass, or -1 for the unfused sequence (two forward
+ * transforms, a product kernel, a backward transform). */
+int heffte_gb300_convolve_route(heffte_gb300_plan plan, int prec, int two_inputs, int *fused_dim);
+int heffte_gb300_convolve(heffte_gb300_plan plan, int prec, const void *x, const void *y, void *output,
+                          void *workspace, int scale);
+
 /* ======================================================================= */
 /* 4. Batches of many small boxes of uneven sizes, autotuner                */
 /* ======================================================================= */
@@ -288,6 +309,10 @@ int heffte_gb300_plan_set_knobs(heffte_gb300_plan plan, int variant, int tile_di
  * reference, whose GPU backends call cuFFT / rocFFT / oneMKL
  * (src/heffte_backend_cuda.cu). */
 int heffte_gb300_plan_set_tensor_cores(heffte_gb300_plan plan, int enable);
+/* enable = 1 (default): convolve takes its fused route where it applies;
+ * 0: always the unfused sequence (forward transforms, product kernel,
+ * backward transform), the reference's order of operations. */
+int heffte_gb300_plan_set_convolution_fusion(heffte_gb300_plan plan, int enable);
 /* The 18 features the selector reads for a transform of `kind` and `prec`. */
 int heffte_gb300_plan_features(int kind, int prec, const int size[3], float *features);
 /* Candidate c in [0, 16): use_reorder = c & 1, variant = (c >> 1) & 1,

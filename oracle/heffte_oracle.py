@@ -120,6 +120,29 @@ def fft3d_c2r(x, size, r2c_dir, in_order=(0, 1, 2), out_order=(0, 1, 2), scaling
     return from_canonical(y, out_order)
 
 
+def convolve(x, y, size, r2c_dir=None, order=(0, 1, 2), scaling=SCALE_FULL):
+    """backward(forward(x) .* forward(y)) with the backward scaling: the step of
+    benchmarks/convolution.cpp:89-95 (forward, pointwise product, backward)
+    with both forward transforms unscaled.  y None: x .* x.  r2c_dir None:
+    complex arrays through fft3d; else real arrays through fft3d_r2c (the
+    product on the half spectrum)."""
+    n = int(np.prod(size))
+    if r2c_dir is None:
+        fx = fft3d_c2c(x, size, order, order)
+        fy = fx if y is None else fft3d_c2c(y, size, order, order)
+        return fft3d_c2c(fx * fy, size, order, order, direction=1, scaling=scaling)
+    fx = fft3d_r2c(x, size, r2c_dir, order, order)
+    fy = fx if y is None else fft3d_r2c(y, size, r2c_dir, order, order)
+    return fft3d_c2r(fx * fy, size, r2c_dir, order, order, scaling=scaling)
+
+
+def convolution_benchmark_step(x, size):
+    """The in-place step timed by benchmarks/convolution.cpp:89-95:
+    forward with scale::full, X .* X, backward unscaled."""
+    f = fft3d_c2c(x, size, scaling=SCALE_FULL)
+    return fft3d_c2c(f * f, size, direction=1)
+
+
 def _r2r_forward_1d(kind, x):
     """Forward r2r along the last axis through the extended signal
     (cpu_*_pre_pos_processor::pre_forward/post_forward)."""

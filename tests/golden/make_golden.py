@@ -16,9 +16,12 @@ Cases:
   (bit-exact cases) for 4, 8 and 16 byte elements;
 * ``c2c64.npz`` — the 64x64x64 complex<double> forward+backward case with
   re/im uniform [-1, 1) from seed 64: the output sampled at 4096 seeded
-  positions plus its L2 norm (the full arrays are regenerated from the seed).
+  positions plus its L2 norm (the full arrays are regenerated from the seed);
+* ``convolution.npz`` — the convolution benchmark's step (forward scale::full,
+  X .* X, backward) and a two-input circular convolution, complex<float> and
+  complex<double>, computed by the reference's transforms.
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [fixture ...]
 """
 import ctypes
 import os
@@ -210,11 +213,36 @@ def c2c64():
             "bwd_sample": z[pos], "roundtrip_err": np.array(np.abs(z - x).max())}
 
 
+def convolution():
+    """The step of benchmarks/convolution.cpp:89-95 run through the reference:
+    forward with scale::full, the product X .* X (the benchmark's host loop,
+    restated here with numpy), backward unscaled; and the two-input form
+    with both forward transforms unscaled and the backward one scale::full."""
+    out = {}
+    rng = np.random.default_rng(95)
+    for tag, size, dt in (("f", (16, 12, 10), np.complex64), ("d", (16, 12, 10), np.complex128),
+                          ("d2", (32, 8, 6), np.complex128)):
+        n = int(np.prod(size))
+        x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(dt)
+        y = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(dt)
+        fx = ref_c2c(x, size, (0, 1, 2), (0, 1, 2), 0, 1)
+        step = ref_c2c((fx * fx).astype(dt), size, (0, 1, 2), (0, 1, 2), 1, 0)
+        gx = ref_c2c(x, size, (0, 1, 2), (0, 1, 2), 0, 0)
+        gy = ref_c2c(y, size, (0, 1, 2), (0, 1, 2), 0, 0)
+        conv = ref_c2c((gx * gy).astype(dt), size, (0, 1, 2), (0, 1, 2), 1, 1)
+        out.update({tag + "_size": np.array(size), tag + "_x": x, tag + "_y": y, tag + "_step": step,
+                    tag + "_conv": conv})
+    return out
+
+
+FIXTURES = {"known_answers": known_answers, "seeded": seeded, "packers": packers, "c2c64": c2c64,
+            "convolution": convolution}
+
+
 def main():
-    np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **known_answers())
-    np.savez_compressed(os.path.join(HERE, "seeded.npz"), **seeded())
-    np.savez_compressed(os.path.join(HERE, "packers.npz"), **packers())
-    np.savez_compressed(os.path.join(HERE, "c2c64.npz"), **c2c64())
+    names = sys.argv[1:] or list(FIXTURES)
+    for name in names:
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **FIXTURES[name]())
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
