@@ -457,6 +457,9 @@ WORKLOADS = {
     "conv512": ("conv", (512, 512, 512), 0, "self"),
     "conv512unfused": ("conv", (512, 512, 512), 0, "self-unfused"),
     "conv512xy": ("conv", (512, 512, 512), 0, "xy"),
+    # small case (256 MiB, above L2) for ncu captures of the fused convolution
+    # pass on 512-point columns
+    "conv256x256x512": ("conv", (256, 256, 512), 0, "self"),
 }
 
 BATCH_SIDES = [16, 24, 32, 40, 48, 64, 80, 96, 128]

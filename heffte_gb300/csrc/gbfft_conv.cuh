@@ -7,7 +7,7 @@
 // without leaving shared memory, so the spectrum is never written to HBM and
 // the product costs no pass of its own.  Column tiles come in by 3-D
 // tensor-map copies (one map per operand, both completing on the tile's
-// mbarrier, bounded waits) and are double buffered as in the pipelined
+// mbarrier, bounded waits) into two or three slots as in the pipelined
 // transforms; every radix stage runs in place in the tile.
 #pragma once
 #include <cuda.h>
@@ -38,8 +38,15 @@ __host__ __device__ constexpr int conv_tpb(int N, int csize, bool two){
     return tpb;
 }
 __host__ __device__ constexpr int conv_threads(int N, int csize, bool two){ return conv_tpb(N, csize, two) * pipe_tt(N); }
+// tile slots per operand: three (two tiles in flight while one is
+// transformed) for a self-convolution whose two slots already take more than
+// half of an SM's shared memory, two otherwise
+__host__ __device__ constexpr int conv_nbuf(int N, int csize, bool two){
+    return (!two && 2 * N * conv_tpb(N, csize, two) * csize > 114 * 1024 &&
+            3 * N * conv_tpb(N, csize, two) * csize <= 200 * 1024) ? 3 : 2;
+}
 __host__ __device__ constexpr int conv_smem(int N, int csize, bool two){
-    return (two ? 4 : 2) * N * conv_tpb(N, csize, two) * csize;
+    return (two ? 2 : 1) * conv_nbuf(N, csize, two) * N * conv_tpb(N, csize, two) * csize;
 }
 
 // The last forward stage L of the pipelined radix plan of one column, in
@@ -120,16 +127,17 @@ k_conv_cols(ConvParams P, const __grid_constant__ CUtensorMap tmx, const __grid_
     constexpr int TILE = N * TPB;                       // complex values per tile buffer
     constexpr int BOXR = (N < 256) ? N : 256;           // rows per tensor-map copy
     constexpr int WPE = (int)sizeof(C) / 8;             // 8-byte tensor words per value
+    constexpr int NBUF = conv_nbuf(N, (int)sizeof(C), TWO);
     extern __shared__ __align__(128) unsigned char smraw[];
-    C *tiles = reinterpret_cast<C*>(smraw);             // x tiles [0], [1]; y tiles [2], [3]
-    __shared__ __align__(8) uint64_t bar[2];
+    C *tiles = reinterpret_cast<C*>(smraw);             // x tiles [0, NBUF), y tiles [NBUF, 2 NBUF)
+    __shared__ __align__(8) uint64_t bar[NBUF];
     int const tid = threadIdx.x, warp = tid >> 5;
     int const loc = tid % TPB, t = tid / TPB;
     Layout const L = P.L;
 
     if (tid == 0){
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        #pragma unroll
+        for (int i = 0; i < NBUF; i++) mbar_init(&bar[i], 1);
         fence_mbar_init();
         prefetch_tmap(&tmx);
         if (TWO) prefetch_tmap(&tmy);
@@ -156,28 +164,33 @@ k_conv_cols(ConvParams P, const __grid_constant__ CUtensorMap tmx, const __grid_
         // out-of-range columns are zero-filled and still count as transferred bytes
         mbar_arrive_expect_tx(&bar[b], (uint32_t)((TWO ? 2 : 1) * TILE * sizeof(C)));
         load(&tmx, tiles + b * TILE, blk, c0, &bar[b]);
-        if (TWO) load(&tmy, tiles + (2 + b) * TILE, blk, c0, &bar[b]);
+        if (TWO) load(&tmy, tiles + (NBUF + b) * TILE, blk, c0, &bar[b]);
     };
 
-    uint32_t ph0 = 0, ph1 = 0;
+    uint32_t phase = 0;                                 // bit b: parity of the next wait on bar[b]
     long long tile = blockIdx.x;
-    if (tile < P.ntiles) issue(tile, 0);
+    #pragma unroll
+    for (int i = 0; i < NBUF - 1; i++){
+        long long tl = tile + (long long)i * gridDim.x;
+        if (tl < P.ntiles) issue(tl, i);
+    }
     T const sc = (T)P.scale;
     C const *tw = reinterpret_cast<C const*>(P.tw);
     C *out = reinterpret_cast<C*>(P.x);
     for (int it = 0; tile < P.ntiles; tile += gridDim.x, it++){
-        int b = it & 1;
-        long long nxt = tile + gridDim.x;
+        int b = it % NBUF;
+        // the tile NBUF - 1 ahead goes into the slot consumed last iteration
+        long long nxt = tile + (long long)(NBUF - 1) * gridDim.x;
         if (nxt < P.ntiles){
             if (warp == 0) fence_proxy_async_smem();
-            issue(nxt, b ^ 1);
+            issue(nxt, (it + NBUF - 1) % NBUF);
         }
-        bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0, P.status);
+        bool ok = mbar_wait_bounded(&bar[b], (phase >> b) & 1u, P.status);
         if (__syncthreads_or(!ok)) return;
-        if (b) ph1 ^= 1; else ph0 ^= 1;
+        phase ^= 1u << b;
 
         C *tx = tiles + b * TILE;
-        C *ty = tiles + (2 + b) * TILE;
+        C *ty = tiles + (NBUF + b) * TILE;
         long long blk, c0;
         tile_origin(tile, blk, c0);
         long long const ca = c0 + loc;

@@ -90,9 +90,19 @@ __host__ __device__ constexpr int pipe_tile_elems(int N, int tpb, int kind){
     return (kind == PK_C2R_BWD || kind == PK_R2C_FWD)
            ? ((pipe_c2r_pitch(N) * 2 * tpb > N * tpb) ? pipe_c2r_pitch(N) * 2 * tpb : N * tpb) : N * tpb;
 }
-__host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind){
+// Tile buffers: three (two tiles in flight while one is transformed) for c2c
+// column tiles of the tensor-map loader whose two buffers already take more
+// than half of an SM's shared memory (one CTA per SM, so a deeper prefetch is
+// what keeps more copies in flight), two otherwise.
+__host__ __device__ constexpr int pipe_nbuf(int N, int csize, bool cols, int kind, int loader){
+    return (cols && loader == LD_TENSOR && (kind == PK_C2C_FWD || kind == PK_C2C_BWD) &&
+            2 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize > 114 * 1024 &&
+            3 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize <= 200 * 1024) ? 3 : 2;
+}
+__host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind, int loader){
     int tpb = pipe_tpb(N, csize, cols);
-    return 2 * pipe_tile_elems(N, tpb, kind) * csize + (cols ? 0 : tpb * pipe_padn(N) * csize);
+    return pipe_nbuf(N, csize, cols, kind, loader) * pipe_tile_elems(N, tpb, kind) * csize +
+           (cols ? 0 : tpb * pipe_padn(N) * csize);
 }
 
 struct PipeParams {
@@ -204,11 +214,13 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     constexpr int WIDTH = PAIRED ? 2 * TPB : TPB;           // input elements per tile row (columns)
     constexpr bool FWD = (KIND == PK_C2C_FWD || KIND == PK_R2C_FWD || KIND == PK_R2R_FWD);
     constexpr int PADN = pipe_padn(N);
+    constexpr int NBUF = pipe_nbuf(N, (int)sizeof(C), COLS, KIND, LOADER);
+    static_assert(LOADER != LD_CPASYNC || NBUF == 2, "cp.async tiles are double buffered");
 
     extern __shared__ __align__(128) unsigned char smraw[];
     C *tiles = reinterpret_cast<C*>(smraw);
-    C *xline = tiles + 2 * TILE;     // line tiles: padded exchange buffer
-    __shared__ __align__(8) uint64_t bar[2];
+    C *xline = tiles + NBUF * TILE;  // line tiles: padded exchange buffer
+    __shared__ __align__(8) uint64_t bar[NBUF];
 
     int tid = threadIdx.x;
     int loc, t;
@@ -218,8 +230,8 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     int units_per = PAIRED ? 2 : 1;
 
     if (LOADER != LD_CPASYNC && tid == 0){
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        #pragma unroll
+        for (int i = 0; i < NBUF; i++) mbar_init(&bar[i], 1);
         fence_mbar_init();
     }
     if (LOADER == LD_TENSOR && tid == 0) prefetch_tmap(&tmap);
@@ -298,27 +310,33 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         }
     };
 
-    uint32_t ph0 = 0, ph1 = 0;
+    uint32_t phase = 0;              // bit b: parity of the next wait on bar[b]
     long long tile = blockIdx.x;
-    if (tile < P.ntiles) issue(tile, 0);
+    // the first NBUF - 1 tiles of this CTA
+    #pragma unroll
+    for (int i = 0; i < NBUF - 1; i++){
+        long long tl = tile + (long long)i * gridDim.x;
+        if (tl < P.ntiles) issue(tl, i);
+    }
     T sc = (T)P.scale;
     for (int it = 0; tile < P.ntiles; tile += gridDim.x, it++){
-        int b = it & 1;
-        long long nxt = tile + gridDim.x;
+        int b = it % NBUF;
+        // the tile NBUF - 1 ahead goes into the buffer consumed last iteration
+        long long nxt = tile + (long long)(NBUF - 1) * gridDim.x;
         if (nxt < P.ntiles){
             if (LOADER != LD_CPASYNC && warp == 0) fence_proxy_async_smem();
-            issue(nxt, b ^ 1);
+            issue(nxt, (it + NBUF - 1) % NBUF);
         }
         if constexpr (LOADER == LD_CPASYNC){
             if (nxt < P.ntiles) cp_async_wait<1>(); else cp_async_wait<0>();
             __syncthreads();
         } else {
-            bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0, P.status);
+            bool ok = mbar_wait_bounded(&bar[b], (phase >> b) & 1u, P.status);
             if (__syncthreads_or(!ok)){
                 if (P.bulk_store && tid == 0) bulk_wait<0>();
                 return;
             }
-            if (b) ph1 ^= 1; else ph0 ^= 1;
+            phase ^= 1u << b;
         }
 
         C *tb = tiles + b * TILE;

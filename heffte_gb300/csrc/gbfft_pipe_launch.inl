@@ -19,7 +19,7 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     using C = c_t<T>;
     constexpr bool PAIRED = pipe_paired(KIND);
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
-    constexpr int SMEM = pipe_smem(N, sizeof(C), COLS, KIND);
+    constexpr int SMEM = pipe_smem(N, sizeof(C), COLS, KIND, LOADER);
     static_assert(SMEM <= 227 * 1024, "pipelined tile exceeds the shared memory of a CTA");
     constexpr int THREADS = pipe_threads(N, sizeof(C), COLS);
     constexpr int IN_ES = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) ? (int)sizeof(T) : (int)sizeof(C);
