@@ -321,7 +321,18 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
     bool cols = !(Li.estride == 1 && Lo.estride == 1);
     if (!cols && (Li.estride != 1)) return false;
     merge_blocks(Li, Lo, G);
+    // column tiles whose input blocks are contiguous but whose output blocks
+    // are not (a padded pitch on one side): merge the input's alone, so that
+    // tiles span whole planes and a plane stride that is no multiple of 16
+    // bytes does not keep the tensor-map loader out
+    int out_split = 0;
+    if (cols && Li.count != G && Li.bstride == Li.count * Li.dist && in != out){
+        Li.count = G;
+        Li.bstride = G * Li.dist;
+        out_split = 1;
+    }
     PipeLaunch a{};
+    a.out_split = out_split;
     a.Li = Li; a.Lo = Lo; a.in = in; a.out = out;
     a.tw = f.twiddles(prec, s);
     a.rtw = (kind == K_R2R_F || kind == K_R2R_B) ? f.r2r_twiddles(prec, s) : nullptr;

@@ -128,6 +128,7 @@ struct PipeLaunch {
     long long G;
     double scale;
     int sine;
+    int out_split;      // column tiles: Li's blocks merged into one, Lo's kept (output offsets by division)
     int *status;
 };
 // Pipelined complex transforms of any supported length (runtime radix plan,

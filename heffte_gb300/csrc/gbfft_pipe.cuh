@@ -120,6 +120,7 @@ struct PipeParams {
     int tswap;
     int line_pitch;         // line tiles: input elements per line (the line length, or padded for c2r)
     int bulk_store;         // c2c line tiles: results staged in the tile buffer, one bulk store per tile
+    int out_split;          // column tiles: the input's blocks are merged into one, the output's are not
     int *status;
 };
 
@@ -351,8 +352,14 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             long long ca = c0 + (long long)loc * units_per;
             va = ca < Li.count;
             vb = PAIRED ? (ca + 1 < Li.count) : false;
-            oa = blk * Lo.bstride + ca * Lo.dist;
-            obb = oa + Lo.dist;
+            if (P.out_split){
+                // ca counts columns over all blocks of the output
+                if (va) oa = base_of_fast(Lo, ca);
+                if (vb) obb = base_of_fast(Lo, ca + 1);
+            } else {
+                oa = blk * Lo.bstride + ca * Lo.dist;
+                obb = oa + Lo.dist;
+            }
         } else {
             long long ga = c0 + (long long)loc * units_per, gb = ga + 1;
             va = ga < P.G;

@@ -89,6 +89,7 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     }
     P.Li = a.Li; P.Lo = a.Lo; P.in = a.in; P.out = a.out; P.tw = a.tw; P.rtw = a.rtw;
     P.G = a.G; P.scale = a.scale; P.do_scale = (a.scale != 1.0); P.sine = a.sine; P.status = a.status;
+    P.out_split = a.out_split;
     if (COLS){
         P.tiles_per_block = (Li.count + WIDTH - 1) / WIDTH;
         P.ntiles = blocks * P.tiles_per_block;

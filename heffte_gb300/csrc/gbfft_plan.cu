@@ -304,14 +304,21 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         p->scale_factor = dct1 ? 1.0 / (64.0 * n1) : (r2r ? 1.0 / (64.0 * n) : 1.0 / n);
     } else {
         Box3 cgeom = inbox.r2c(r2c_dir);
-        std::vector<PassSpec> fwd{{K_R2C, r2c_dir}}, bwd;
-        for (int i = 0; i < 3; i++) if (io[i] != r2c_dir) fwd.push_back({K_C2C_F, io[i]});
-        for (int i = 0; i < 3; i++) if (oo[i] != r2c_dir) bwd.push_back({K_C2C_B, oo[i]});
-        bwd.push_back({K_C2R, r2c_dir});
         // the complex intermediate goes through a padded workspace when its
         // fastest extent is odd (plans without reshapes)
         bool pad_f = !reorder && (cgeom.size[io[0]] % 2 == 1);
         bool pad_b = !reorder && (cgeom.size[oo[0]] % 2 == 1);
+        std::vector<PassSpec> fwd{{K_R2C, r2c_dir}}, bwd;
+        for (int i = 0; i < 3; i++) if (io[i] != r2c_dir) fwd.push_back({K_C2C_F, io[i]});
+        // backward c2c passes: with a padded workspace the slowest dimension
+        // goes first, so that the caller's unpadded half spectrum (rows of an
+        // odd number of values, not 16-byte aligned) is read by the pass
+        // whose batch planes are contiguous, which merges them into one and
+        // loads its column tiles by tensor map; the order of the separable
+        // passes changes rounding only
+        if (pad_b){ for (int i = 2; i >= 0; i--) if (oo[i] != r2c_dir) bwd.push_back({K_C2C_B, oo[i]}); }
+        else { for (int i = 0; i < 3; i++) if (oo[i] != r2c_dir) bwd.push_back({K_C2C_B, oo[i]}); }
+        bwd.push_back({K_C2R, r2c_dir});
         p->fwd = build_ops(fwd, inbox, outbox, cgeom, reorder, true, false, wf, knobs.radix_policy, false, pad_f);
         p->fwd_alias = build_ops(fwd, inbox, outbox, cgeom, reorder, true, true, wfa, knobs.radix_policy, false, pad_f);
         p->bwd = build_ops(bwd, outbox, inbox, cgeom, reorder, false, false, wb, knobs.radix_policy, false, pad_b);
