@@ -443,6 +443,8 @@ WORKLOADS = {
     "z2z64": ("c2c", (64, 64, 64), 1),
     # small case (256 MiB, above L2) for ncu captures of the c2c pass kernels
     "c2c512x512x128": ("c2c", (512, 512, 128), 0),
+    # small case (256 MiB real input, above L2) for ncu captures of the r2c line pass
+    "r2c512x512x256": ("r2c", (512, 512, 256), 0),
     # 256 r2c float boxes, sides i.i.d. from {16, 24, ..., 128} (seed 256), one persistent launch
     "batch256": ("batch", None, 0),
     # the same after autotuning the radix plan / tile size of every side length
@@ -457,6 +459,9 @@ WORKLOADS = {
     "conv512": ("conv", (512, 512, 512), 0, "self"),
     "conv512unfused": ("conv", (512, 512, 512), 0, "self-unfused"),
     "conv512xy": ("conv", (512, 512, 512), 0, "xy"),
+    # the same on real data through an r2c plan (the product on the half spectrum)
+    "conv512r2c": ("conv", (512, 512, 512), 0, "r2c-self"),
+    "conv512r2cunfused": ("conv", (512, 512, 512), 0, "r2c-self-unfused"),
     # small case (256 MiB, above L2) for ncu captures of the fused convolution
     # pass on 512-point columns
     "conv256x256x512": ("conv", (256, 256, 512), 0, "self"),
@@ -594,26 +599,32 @@ def run_selector_workload(name):
 
 
 def run_conv_workload(name, steps, warmup):
-    """plan.convolve on a c2c box: time per convolution, GFLOP/s counting
-    its transforms (5 N log2 N each: 2 for x .* x, 3 for x .* y), the bytes of
-    its passes against the HBM peak, and the result against this library's
-    complex<double> convolution of the same input (the FP64 path the parity
-    tests hold to 1e-12 of the FP64 oracle)."""
+    """plan.convolve on a c2c (or r2c) box: time per convolution, GFLOP/s
+    counting its transforms (5 N log2 N each: 2 for x .* x, 3 for x .* y), the
+    bytes of its passes against the HBM peak, and the result against this
+    library's double-precision convolution of the same input (the FP64 path
+    the parity tests hold to 1e-12 of the FP64 oracle)."""
     import torch
     import heffte_gb300 as gb
     _, size, prec, form = WORKLOADS[name]
     N = size[0] * size[1] * size[2]
+    real = form.startswith("r2c")
+    two = form == "xy"
     stream = torch.cuda.current_stream()
     box = gb.box3d((0, 0, 0), [s - 1 for s in size])
-    plan = gb.fft3d(box, box, stream=stream)
-    if form == "self-unfused":
+
+    def make_plan():
+        return gb.fft3d_r2c(box, box.r2c(0), 0, stream=stream) if real else gb.fft3d(box, box, stream=stream)
+    plan = make_plan()
+    if form.endswith("unfused"):
         plan.set_convolution_fusion(False)
-    two = form == "xy"
     rdt = torch.float32 if prec == 0 else torch.float64
     gen = torch.Generator(device="cuda")
     gen.manual_seed(99)
 
     def rand():
+        if real:
+            return torch.randn(N, device="cuda", generator=gen, dtype=rdt)
         return torch.complex(torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1,
                              torch.rand(N, device="cuda", generator=gen, dtype=rdt) * 2 - 1)
     x = rand()
@@ -621,7 +632,8 @@ def run_conv_workload(name, steps, warmup):
     # out of place: the benchmark's in-place loop feeds each result back in,
     # which under- or overflows after a few steps; the passes are the same
     out = torch.empty_like(x)
-    work = torch.empty(plan.convolve_workspace(), dtype=x.dtype, device="cuda")
+    cdt = torch.complex64 if prec == 0 else torch.complex128
+    work = torch.empty(plan.convolve_workspace(), dtype=cdt, device="cuda")
     route = plan.convolve_route(prec, two)
 
     def step():
@@ -638,23 +650,32 @@ def run_conv_workload(name, steps, warmup):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     ntrans = 3 if two else 2
-    cs = 8 if prec == 0 else 16
-    # passes over the box in units of N complex values moved (read or write):
-    # fused self 5 passes (10); fused xy 2 + 2 forward passes, the fused pass
-    # (2 reads, 1 write), 2 backward passes (15); unfused self 3 + 3 transform
-    # passes and the product's read + write (14; 18 with y's forward and read)
-    units = (15 if two else 10) if route >= 0 else (18 if two else 14)
-    b = units * N * cs
+    rs, cs = (4, 8) if prec == 0 else (8, 16)
+    if real:
+        # r2c: the real passes read / write N reals, the complex ones move the
+        # (unpadded) half spectrum Nc; fused: r2c, c2c, fused, c2c, c2r;
+        # unfused: r2c, 2 c2c, product, 2 c2c, c2r
+        nc = (size[0] // 2 + 1) * size[1] * size[2]
+        b = 2 * N * rs + (8 if route >= 0 else 12) * nc * cs
+    else:
+        # passes over the box in units of N complex values moved (read or
+        # write): fused self 5 passes (10); fused xy 2 + 2 forward passes, the
+        # fused pass (2 reads, 1 write), 2 backward passes (15); unfused self
+        # 3 + 3 transform passes and the product's read + write (14; 18 with
+        # y's forward and read)
+        units = (15 if two else 10) if route >= 0 else (18 if two else 14)
+        b = units * N * cs
     peak, _ = peaks()
     del work
-    x64 = x.to(torch.complex128)
-    y64 = y.to(torch.complex128) if two else None
+    hdt = torch.float64 if real else torch.complex128
+    x64 = x.to(hdt)
+    y64 = y.to(hdt) if two else None
     o64 = torch.empty_like(x64)
-    gb.fft3d(box, box, stream=stream).convolve(x64, y64, o64, gb.scale.full)
-    err = float((torch.linalg.vector_norm(out.to(torch.complex128) - o64) / torch.linalg.vector_norm(o64)).item())
+    make_plan().convolve(x64, y64, o64, gb.scale.full)
+    err = float((torch.linalg.vector_norm(out.to(hdt) - o64) / torch.linalg.vector_norm(o64)).item())
     return {"workload": name, "form": form, "fused_dim": route, "ms_per_step": ms,
             "gflops": ntrans * flops_per_transform(N) / (ms / 1e3) / 1e9,
-            "pass_units": units, "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak,
+            "bytes_per_step": b, "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak,
             "rel_l2_vs_fp64": err}
 
 

@@ -438,53 +438,84 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
 // ---------------------------------------------------------------------------
 // convolution (benchmarks/convolution.cpp: forward, pointwise product, backward)
 // ---------------------------------------------------------------------------
-// Fused route (c2c, no reshapes, the same order on both sides): the forward
-// passes along two dimensions, then ONE pass along the third that transforms
-// each column forward, multiplies it by y's column (or squares it), scales and
-// transforms it back (gbfft_conv.cuh), then the backward passes along the two
-// other dimensions.  Five passes over the box for a self-convolution where
-// the unfused sequence makes six transform passes and a product pass.
-int Plan3D::convolve_fused_dim(int prec, void *out, void const *wy) const{
-    if (kind != PK_C2C || opts.use_reorder || inbox.order != outbox.order) return -1;
+// Fused route (no reshapes, the same order on both sides; r2c plans with the
+// r2c along the fastest dimension): the forward passes along two dimensions
+// (for r2c: the r2c pass, then a c2c pass on the half spectrum), then ONE
+// pass along the third that transforms each column forward, multiplies it by
+// y's column (or squares it), scales and transforms it back (gbfft_conv.cuh),
+// then the backward passes along the two other dimensions.  Five passes over
+// the (half-spectrum) box for a self-convolution where the unfused sequence
+// makes six transform passes and a product pass.
+
+// The box the spectra live in: the c2c box itself, or the r2c half spectrum
+// with padded rows (padded_pitch), whose column tiles load by tensor map.
+Box3 Plan3D::conv_box() const{
+    if (kind != PK_R2C) return inbox;
+    Box3 b = inbox.r2c(r2c_dir);
+    b.pitch0 = padded_pitch(b.size[b.order[0]]);
+    return b;
+}
+
+// offsets of the spectrum boxes in the workspace, rounded to 32 elements
+// (256 bytes) so that they keep the alignment of the workspace itself
+static long long round32(long long n){ return (n + 31) / 32 * 32; }
+
+long long Plan3D::convolve_workspace() const{
+    return round32(work_elems) + 2 * round32(std::max(conv_box().alloc_count(), size_outbox()));
+}
+
+int Plan3D::convolve_fused_dim(int prec, void *xb, void const *yb) const{
+    if (kind != PK_C2C && kind != PK_R2C) return -1;
+    if (opts.use_reorder || inbox.order != outbox.order) return -1;
+    if (kind == PK_R2C && r2c_dir != inbox.order[0]) return -1;
     if (!knobs.conv_fused || knobs.tensor_cores || knobs.variant == 1 || knobs.radix_policy != 0) return -1;
-    Box3 const &B = inbox;
+    Box3 const B = conv_box();
     for (int d = 0; d < 3; d++) if (B.size[d] < 2) return -1;
     for (int fi : {2, 1}){
         int f = B.order[fi];
         auto ff = get_fft1d((int)B.size[f]);
-        if (launch_conv_pass(stream, *ff, prec, pass_layout(B, f, B.order), out, wy, B.count() / B.size[f], 1.0, true))
+        if (launch_conv_pass(stream, *ff, prec, pass_layout(B, f, B.order), xb, yb, B.count() / B.size[f], 1.0, true))
             return f;
     }
     return -1;
 }
 
-bool Plan3D::convolve_fused(int prec, void const *x, void const *y, void *out, void *wy, double scale){
-    int f = convolve_fused_dim(prec, out, y ? wy : nullptr);
+bool Plan3D::convolve_fused(int prec, void const *x, void const *y, void *out, void *w1, void *w2, double scale){
+    bool const r2c = (kind == PK_R2C);
+    // spectra: c2c in the output (x) and the first workspace box (y);
+    // r2c in the two workspace boxes
+    void *xb = r2c ? w1 : out;
+    void *yb = y ? (r2c ? w2 : w1) : nullptr;
+    int f = convolve_fused_dim(prec, xb, yb);
     if (f < 0) return false;
-    Box3 const &B = inbox;
+    Box3 const B = conv_box();
     std::array<int, 3> const io = B.order;
     LaunchCfg cfg;
-    {
-        int rest[2], k = 0;
-        for (int i = 0; i < 3; i++) if (io[i] != f) rest[k++] = io[i];
-        auto ff = get_fft1d((int)B.size[f]);
-        Layout Lf = pass_layout(B, f, io);
-        long long Gf = B.count() / B.size[f];
-        auto f0 = get_fft1d((int)B.size[rest[0]]), f1 = get_fft1d((int)B.size[rest[1]]);
-        Layout L0 = pass_layout(B, rest[0], io), L1 = pass_layout(B, rest[1], io);
-        long long G0 = B.count() / B.size[rest[0]], G1 = B.count() / B.size[rest[1]];
-        // y first: y may alias out
-        if (y){
-            launch_c2c(stream, *f0, prec, true, L0, L0, y, wy, G0, 1.0, cfg);
-            launch_c2c(stream, *f1, prec, true, L1, L1, wy, wy, G1, 1.0, cfg);
-        }
-        launch_c2c(stream, *f0, prec, true, L0, L0, x, out, G0, 1.0, cfg);
-        launch_c2c(stream, *f1, prec, true, L1, L1, out, out, G1, 1.0, cfg);
-        if (!launch_conv_pass(stream, *ff, prec, Lf, out, y ? wy : nullptr, Gf, scale, false))
-            throw Error(ST_CUDA, "fused convolution pass refused after its check passed");
-        launch_c2c(stream, *f1, prec, false, L1, L1, out, out, G1, 1.0, cfg);
-        launch_c2c(stream, *f0, prec, false, L0, L0, out, out, G0, 1.0, cfg);
+    int rest[2], k = 0;
+    for (int i = 0; i < 3; i++) if (io[i] != f) rest[k++] = io[i];
+    int const d0 = rest[0], d1 = rest[1];
+    auto ff = get_fft1d((int)B.size[f]);
+    auto f1 = get_fft1d((int)B.size[d1]);
+    auto f0 = get_fft1d((int)inbox.size[d0]);       // the real length for r2c
+    Layout const Lf = pass_layout(B, f, io), L1 = pass_layout(B, d1, io);
+    Layout const L0c = pass_layout(B, d0, io), L0r = pass_layout(inbox, d0, io);
+    long long const Gf = B.count() / B.size[f], G1 = B.count() / B.size[d1], G0 = inbox.count() / inbox.size[d0];
+    auto first = [&](void const *src, void *dst){
+        if (r2c) launch_r2c(stream, *f0, prec, L0r, L0c, src, dst, G0, 1.0, cfg);
+        else launch_c2c(stream, *f0, prec, true, L0c, L0c, src, dst, G0, 1.0, cfg);
+    };
+    // y first: y may alias out
+    if (y){
+        first(y, yb);
+        launch_c2c(stream, *f1, prec, true, L1, L1, yb, yb, G1, 1.0, cfg);
     }
+    first(x, xb);
+    launch_c2c(stream, *f1, prec, true, L1, L1, xb, xb, G1, 1.0, cfg);
+    if (!launch_conv_pass(stream, *ff, prec, Lf, xb, yb, Gf, scale, false))
+        throw Error(ST_CUDA, "fused convolution pass refused after its check passed");
+    launch_c2c(stream, *f1, prec, false, L1, L1, xb, xb, G1, 1.0, cfg);
+    if (r2c) launch_c2r(stream, *f0, prec, L0c, L0r, xb, out, G0, 1.0, cfg);
+    else launch_c2c(stream, *f0, prec, false, L0c, L0c, xb, out, G0, 1.0, cfg);
     return true;
 }
 
@@ -507,9 +538,10 @@ void Plan3D::convolve(int prec, void const *x, void const *y, void *out, void *w
         }
         w = static_cast<char*>(conv_cache);
     }
-    char *w1 = w + (size_t)work_elems * ces;          // spectrum of x
-    char *w2 = w1 + (size_t)size_outbox() * ces;      // spectrum of y
-    if (convolve_fused(prec, x, self ? nullptr : y, out, w1, get_scale(scaling))) return;
+    long long const box = round32(std::max(conv_box().alloc_count(), size_outbox()));
+    char *w1 = w + (size_t)round32(work_elems) * ces; // spectrum of x
+    char *w2 = w1 + (size_t)box * ces;                // spectrum of y
+    if (convolve_fused(prec, x, self ? nullptr : y, out, w1, w2, get_scale(scaling))) return;
     // unfused: both forward transforms, the product kernel, the backward
     // transform carrying the scale
     if (!self) execute(true, prec, 1, y, w2, w, 0);

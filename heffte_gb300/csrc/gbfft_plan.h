@@ -128,14 +128,18 @@ struct Plan3D {
     void execute(bool forward, int prec, int batch, void const *in, void *out, void *work, int scaling);
     // Circular convolution through the plan's transforms (benchmarks/convolution.cpp):
     // out = backward(forward(x) .* forward(y)) with the backward scaling;
-    // y null or equal to x: self-convolution.  Workspace in complex elements.
-    long long convolve_workspace() const { return work_elems + 2 * size_outbox(); }
+    // y null or equal to x: self-convolution.  Workspace in complex elements:
+    // the plan's own, then two spectrum boxes.
+    long long convolve_workspace() const;
     void convolve(int prec, void const *x, void const *y, void *out, void *work, int scaling);
-    // the fused route of convolve for c2c plans; false when it does not apply
-    bool convolve_fused(int prec, void const *x, void const *y, void *out, void *wy, double scale);
+    // the box the spectra of the fused route live in
+    Box3 conv_box() const;
+    // the fused route of convolve; false when it does not apply
+    bool convolve_fused(int prec, void const *x, void const *y, void *out, void *w1, void *w2, double scale);
     // the dimension the fused route transforms in its fused pass (-1: unfused);
-    // only the alignment of out and wy (null: self-convolution) is looked at
-    int convolve_fused_dim(int prec, void *out, void const *wy) const;
+    // only the alignment of the spectrum buffers xb and yb (null: self-
+    // convolution) is looked at
+    int convolve_fused_dim(int prec, void *xb, void const *yb) const;
 };
 
 std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbox, int r2c_dir, Options const &o,
