@@ -192,6 +192,29 @@ def test_gpu_convolution_aliasing_and_scaling(gb, prec):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_convolution_reorder_and_orders(gb, prec):
+    """use_reorder plans and plans whose input and output orders differ take
+    the unfused route; the result is in the input box's order."""
+    import torch
+    size = (32, 16, 64)
+    n = int(np.prod(size))
+    rng = np.random.default_rng(29)
+    x, y = _rand_c(rng, n, prec), _rand_c(rng, n, prec)
+    cases = [((0, 1, 2), (0, 1, 2), True), ((1, 2, 0), (1, 2, 0), True), ((0, 1, 2), (2, 1, 0), False)]
+    for io, oo, reorder in cases:
+        opts = gb.plan_options.default()
+        opts.use_reorder = reorder
+        p = gb.fft3d(gb.box3d((0, 0, 0), [s - 1 for s in size], io), gb.box3d((0, 0, 0), [s - 1 for s in size], oo),
+                     opts)
+        assert p.convolve_route(prec, True) == -1
+        xd, yd = _dev(x), _dev(y)
+        out = torch.empty_like(xd)
+        p.convolve(xd, yd, out, gb.scale.full)
+        assert O.rel_l2(_host(out), O.convolve(x, y, size, order=io)) < TOL[prec], (io, oo, reorder)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("r2c_dir", [0, 1, 2])
 def test_gpu_convolution_r2c(gb, prec, r2c_dir):
     import torch
