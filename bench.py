@@ -462,6 +462,10 @@ WORKLOADS = {
     # the same on real data through an r2c plan (the product on the half spectrum)
     "conv512r2c": ("conv", (512, 512, 512), 0, "r2c-self"),
     "conv512r2cunfused": ("conv", (512, 512, 512), 0, "r2c-self-unfused"),
+    # the location layer (transpose_unpack for the five non-identity maps,
+    # direct_pack / direct_unpack of a 384x512x512 sub-box, scale_data) on a
+    # 512^3 complex<float> array
+    "location512": ("location", (512, 512, 512), 0),
     # small case (256 MiB, above L2) for ncu captures of the fused convolution
     # pass on 512-point columns
     "conv256x256x512": ("conv", (256, 256, 512), 0, "self"),
@@ -520,8 +524,13 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     stream = torch.cuda.current_stream()
     if tune_cache == "loop":
         return run_batch_loop(name, sizes, steps, warmup)
+    plans = None
     if tune_cache is not None:
         gb.tune(0, BATCH_SIDES, tune_cache, stream=stream)
+        plans = {}
+        for n in BATCH_SIDES:
+            rad, tpb, us = gb.tuned_choice(0, n)
+            plans[str(n)] = {"radices": rad, "tpb": tpb, "us_per_tuning_batch": us}
     b = gb.boxbatch(gb.kind.r2c, sizes, 0, stream=stream)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(7)
@@ -550,7 +559,8 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     peak, _ = peaks()
     return {"workload": name, "boxes": len(sizes), "ms_per_step": ms, "gflops": flops / (ms / 1e3) / 1e9,
             "gbs": byts / (ms / 1e3) / 1e9, "hbm_frac": byts / (ms / 1e3) / 1e9 / peak,
-            "roundtrip_max_abs": err, "launches_per_step": 2, "tuned": tune_cache is not None}
+            "roundtrip_max_abs": err, "launches_per_step": 2, "tuned": tune_cache is not None,
+            **({"tuned_plans": plans} if plans else {})}
 
 
 def algorithmic_bytes(kind, size, prec):
@@ -679,6 +689,53 @@ def run_conv_workload(name, steps, warmup):
             "rel_l2_vs_fp64": err}
 
 
+def run_location_workload(name, steps, warmup):
+    """The location layer of the reference's GPU backends (transpose_unpack,
+    direct_pack / direct_unpack, scale_data) through this library's C ABI on a
+    512^3 complex<float> array (1 GiB, above L2): per operation the device time
+    per call and the bytes read + written against the HBM peak."""
+    import torch
+    import heffte_gb300 as gb
+    _, size, prec = WORKLOADS[name][:3]
+    n0, n1, n2 = size
+    N = n0 * n1 * n2
+    stream = torch.cuda.current_stream()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    x = torch.complex(torch.randn(N, device="cuda", generator=gen), torch.randn(N, device="cuda", generator=gen))
+    y = torch.empty_like(x)
+    cf = 2                                      # complex<float> (dtype code of the C ABI)
+    sub = (384, n1, n2)                         # sub-box of the pack / unpack
+    nsub = sub[0] * sub[1] * sub[2]
+    buf = torch.empty(nsub, dtype=torch.complex64, device="cuda")
+    ops = []
+    for mp in ((1, 0, 2), (0, 2, 1), (2, 1, 0), (1, 2, 0), (2, 0, 1)):
+        ops.append(("transpose_unpack map " + "".join(map(str, mp)),
+                    lambda mp=mp: gb.transpose_unpack(cf, n0, n1, n2, n0, n0 * n1, n0, n0 * n1, mp, x, y, stream=stream),
+                    2 * N * 8))
+    ops.append(("direct_pack 384x512x512 of 512^3",
+                lambda: gb.direct_pack(cf, sub[0], sub[1], sub[2], n0, n0 * n1, x, buf, stream=stream), 2 * nsub * 8))
+    ops.append(("direct_unpack 384x512x512 into 512^3",
+                lambda: gb.direct_unpack(cf, sub[0], sub[1], sub[2], n0, n0 * n1, buf, y, stream=stream), 2 * nsub * 8))
+    ops.append(("scale_data 2^28 floats in place", lambda: gb.scale_data(0, 2 * N, x, 1.0, stream=stream), 2 * N * 8))
+    peak, _ = peaks()
+    out = {"workload": name, "ops": []}
+    for label, fn, b in ops:
+        for _ in range(warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        gbs = b / (ms / 1e3) / 1e9
+        out["ops"].append({"op": label, "ms": ms, "bytes": b, "gbs": gbs, "hbm_frac": gbs / peak})
+    return out
+
+
 def run_workload(name, steps, warmup):
     import torch
     import heffte_gb300 as gb
@@ -687,6 +744,8 @@ def run_workload(name, steps, warmup):
         return run_selector_workload(name)
     if kind == "conv":
         return run_conv_workload(name, steps, warmup)
+    if kind == "location":
+        return run_location_workload(name, steps, warmup)
     tc = len(WORKLOADS[name]) > 3 and WORKLOADS[name][3]
     if kind == "batch":
         cache = "loop" if size == "loop" else None
