@@ -19,7 +19,10 @@ a single rank:
   ``include/heffte_fft3d.h:635-650`` (stock/cuFFT tags: 1/(64 N), DCT-I:
   1/(64 prod(n-1)));
 * ``direct_packer`` / ``transpose_packer<tag::cpu>`` and ``data_scaling``
-  (``include/heffte_pack3d.h:83-233``).
+  (``include/heffte_pack3d.h:83-233``);
+* the step of the convolution benchmark (``benchmarks/convolution.cpp:89-95``:
+  forward, pointwise product, backward) and the circular convolution it
+  builds on (``convolve``, ``convolution_benchmark_step``).
 
 The FFTs themselves are numpy's pocketfft in float64 (an FP64 oracle); the
 restated parts are the conventions, layouts and pre/post processing above.
