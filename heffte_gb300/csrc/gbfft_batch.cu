@@ -35,10 +35,20 @@ struct BatchUnit {
 };
 
 enum { DEV_TIMEOUT_DEPENDENCY = 2 };
+// CTAs per SM the batch kernels are compiled for (registers per thread
+// <= 65536 / (256 x this)); float measured best at 4, double kept at 2
+template<typename T> constexpr int batch_ctas_per_sm(){ return sizeof(T) == 4 ? 4 : 2; }
 
-// scaling: 0 none, 1 full (1/N of each box), 2 symmetric
-template<typename T>
-__global__ void __launch_bounds__(256)
+// scaling: 0 none, 1 full (1/N of each box), 2 symmetric.  One kernel per
+// direction: the forward one holds the r2c and forward c2c tile paths, the
+// backward one the backward c2c and c2r paths (fewer paths, fewer
+// registers), compiled for several CTAs per SM: the stage-0 loads of small
+// tiles are latency-bound, and more warps per SM hide them better than the
+// few spills cost (256 uneven r2c float boxes, ms per step: 2.09 at one CTA
+// per SM, 1.54 at two, 1.46 at three, 1.38 at four, 1.64-1.80 at five to
+// eight).
+template<typename T, bool FWD>
+__global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
         long long total_tiles, int *status, int scaling){
@@ -102,34 +112,29 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
         double f = (scaling == 0) ? 1.0 : ((scaling == 1) ? U.scale : sqrt(U.scale));
         T sc = (T)f;
         int dsc = U.last && scaling != 0;
-        switch (U.kind){
-            case K_R2C: {
+        if constexpr (FWD){
+            if (U.kind == K_R2C){
                 T const *in = reinterpret_cast<T const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
                 if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
                 else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                break;
-            }
-            case K_C2R: {
-                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
-                T *out = reinterpret_cast<T*>(dstb) + U.out_off;
-                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                break;
-            }
-            case K_C2C_F: {
+            } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
                 if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
                 else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                break;
             }
-            default: {
+        } else {
+            if (U.kind == K_C2R){
+                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
+                T *out = reinterpret_cast<T*>(dstb) + U.out_off;
+                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+            } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
                 if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
                 else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                break;
             }
         }
         // publish completion of this tile
@@ -152,6 +157,13 @@ Batch::~Batch(){
     if (fwd_graph) cudaGraphDestroy(fwd_graph);
     if (bwd_graph) cudaGraphDestroy(bwd_graph);
     for (void *p : device_allocs) cudaFree(p);
+}
+
+static void const *batch_kernel(int prec, bool fwd){
+    if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true>)
+                              : reinterpret_cast<void const*>(k_batch<float, false>);
+    return fwd ? reinterpret_cast<void const*>(k_batch<double, true>)
+               : reinterpret_cast<void const*>(k_batch<double, false>);
 }
 
 static int tile_tpb(Fft1D const &f, bool cols, bool paired, size_t csize, size_t smem_cap, int tune_tpb){
@@ -319,15 +331,13 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
             smem = std::max(smem, unit * U.tpb);
         }
     b->smem = smem;
-    int nb_sm = 1;
-    if (prec == 0){
-        check_cuda(cudaFuncSetAttribute(k_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, k_batch<float>, kBatchThreads, smem), "occupancy");
-    } else {
-        check_cuda(cudaFuncSetAttribute(k_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, k_batch<double>, kBatchThreads, smem), "occupancy");
+    for (bool fwd : {true, false}){
+        void const *kern = batch_kernel(prec, fwd);
+        int nb_sm = 1;
+        check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, kern, kBatchThreads, smem), "occupancy");
+        (fwd ? b->grid : b->grid_bwd) = std::max(1, nb_sm) * num_sms();
     }
-    b->grid = std::max(1, nb_sm) * num_sms();
     (void)rsize;
     return b;
 }
@@ -358,8 +368,8 @@ static void build_graph(Batch &b, bool fwd){
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
                     &b.args_done, &b.args_total, &b.args_status, &b.args_scaling};
     cudaKernelNodeParams kp{};
-    kp.func = (b.prec == 0) ? reinterpret_cast<void*>(k_batch<float>) : reinterpret_cast<void*>(k_batch<double>);
-    kp.gridDim = dim3((unsigned)b.grid);
+    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd));
+    kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)b.smem;
     kp.kernelParams = args;
@@ -388,8 +398,8 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
                     &args_total, &args_status, &args_scaling};
     cudaKernelNodeParams kp{};
-    kp.func = (prec == 0) ? reinterpret_cast<void*>(k_batch<float>) : reinterpret_cast<void*>(k_batch<double>);
-    kp.gridDim = dim3((unsigned)grid);
+    kp.func = const_cast<void*>(batch_kernel(prec, fwd));
+    kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)smem;
     kp.kernelParams = args;

@@ -47,7 +47,8 @@ struct Batch {
     int nunits = 0;
     long long fwd_tiles = 0, bwd_tiles = 0;
     size_t smem = 0;
-    int grid = 0;
+    int grid = 0;          // persistent CTAs of the forward kernel
+    int grid_bwd = 0;      // and of the backward kernel
     cudaGraph_t fwd_graph = nullptr, bwd_graph = nullptr;
     cudaGraphExec_t fwd_exec = nullptr, bwd_exec = nullptr;
     cudaGraphNode_t fwd_knode = nullptr, bwd_knode = nullptr;
