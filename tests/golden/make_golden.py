@@ -19,7 +19,8 @@ Cases:
   positions plus its L2 norm (the full arrays are regenerated from the seed);
 * ``convolution.npz`` — the convolution benchmark's step (forward scale::full,
   X .* X, backward) and a two-input circular convolution, complex<float> and
-  complex<double>, computed by the reference's transforms.
+  complex<double>, and two-input convolutions of real data through
+  fft3d_r2c, computed by the reference's transforms.
 
 Run:  python tests/golden/make_golden.py [fixture ...]
 """
@@ -231,6 +232,19 @@ def convolution():
         gy = ref_c2c(y, size, (0, 1, 2), (0, 1, 2), 0, 0)
         conv = ref_c2c((gx * gy).astype(dt), size, (0, 1, 2), (0, 1, 2), 1, 1)
         out.update({tag + "_size": np.array(size), tag + "_x": x, tag + "_y": y, tag + "_step": step,
+                    tag + "_conv": conv})
+    # real data through fft3d_r2c (the product on the half spectrum), r2c
+    # along dimension 0 and along dimension 2
+    for tag, size, dt, rd in (("rf", (16, 12, 10), np.float32, 0), ("rd", (16, 12, 10), np.float64, 0),
+                              ("rd2", (12, 10, 16), np.float64, 2), ("rf3", (16, 16, 16), np.float32, 0),
+                              ("rd3", (16, 16, 16), np.float64, 0)):
+        n = int(np.prod(size))
+        x = rng.standard_normal(n).astype(dt)
+        y = rng.standard_normal(n).astype(dt)
+        gx = ref_r2c(x, size, rd, (0, 1, 2), (0, 1, 2), 0, 0)
+        gy = ref_r2c(y, size, rd, (0, 1, 2), (0, 1, 2), 0, 0)
+        conv = ref_r2c((gx * gy).astype(gx.dtype), size, rd, (0, 1, 2), (0, 1, 2), 1, 1)
+        out.update({tag + "_size": np.array(size), tag + "_dir": np.array(rd), tag + "_x": x, tag + "_y": y,
                     tag + "_conv": conv})
     return out
 

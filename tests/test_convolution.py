@@ -54,6 +54,12 @@ def test_oracle_convolution_against_reference(golden):
         tol = 1e-12 if x.dtype == np.complex128 else REF_FLOAT_TOL
         assert O.rel_l2(O.convolution_benchmark_step(x, size), g[tag + "_step"]) < tol, tag
         assert O.rel_l2(O.convolve(x, y, size), g[tag + "_conv"]) < tol, tag
+    # real data through fft3d_r2c
+    for tag in ("rf", "rd", "rd2", "rf3", "rd3"):
+        size = tuple(int(s) for s in g[tag + "_size"])
+        x, y = g[tag + "_x"], g[tag + "_y"]
+        tol = 1e-12 if x.dtype == np.float64 else REF_FLOAT_TOL
+        assert O.rel_l2(O.convolve(x, y, size, r2c_dir=int(g[tag + "_dir"])), g[tag + "_conv"]) < tol, tag
 
 
 def test_convolve_abi_validates(gb):
@@ -121,6 +127,31 @@ def test_gpu_convolution_against_reference(gb, golden):
         ref_tol = 1e-12 if prec == 1 else REF_FLOAT_TOL
         assert O.rel_l2(conv, g[tag + "_conv"]) < ref_tol, tag
         assert O.rel_l2(step, g[tag + "_step"]) < ref_tol, tag
+
+
+@pytest.mark.gpu
+def test_gpu_r2c_convolution_against_reference(gb, golden):
+    """Both routes of an r2c plan against the reference's own r2c convolution
+    (the 16x16x16 cases take the fused route when it is allowed)."""
+    import torch
+    g = golden["convolution"]
+    for tag in ("rf", "rd", "rd2", "rf3", "rd3"):
+        size = tuple(int(s) for s in g[tag + "_size"])
+        rd = int(g[tag + "_dir"])
+        x, y = g[tag + "_x"], g[tag + "_y"]
+        prec = 0 if x.dtype == np.float32 else 1
+        ib = gb.box3d((0, 0, 0), [s - 1 for s in size])
+        for fused in (True, False):
+            p = gb.fft3d_r2c(ib, ib.r2c(rd), rd)
+            p.set_convolution_fusion(fused)
+            if tag.endswith("3"):
+                assert p.convolve_route(prec, True) == (2 if fused else -1)
+            xd, yd = _dev(x), _dev(y)
+            out = torch.empty_like(xd)
+            p.convolve(xd, yd, out, gb.scale.full)
+            got = _host(out)
+            assert O.rel_l2(got, O.convolve(x, y, size, r2c_dir=rd)) < TOL[prec], (tag, fused)
+            assert O.rel_l2(got, g[tag + "_conv"]) < (1e-12 if prec == 1 else REF_FLOAT_TOL), (tag, fused)
 
 
 # (size, order, fused dimension expected for aligned arrays)
