@@ -28,7 +28,7 @@ struct ConvParams {
 };
 
 // columns per tile: the column tile of the pipelined transforms, halved until
-// the double-buffered tiles of every operand fit in shared memory and a tile
+// two tile slots of every operand fit in shared memory and a tile
 // row is at most 256 tensor words (the box limit of a tensor-map copy)
 __host__ __device__ constexpr int conv_tpb(int N, int csize, bool two){
     int tpb = pipe_tpb(N, csize, true);
