@@ -54,6 +54,11 @@ def metric_name():
     return "512^3 c2c fp32 GFLOP/s & %HBM roofline, TC vs plain FP32 at rel-L2<=1e-6"
 
 
+def workload_string(n, prec):
+    """config.workload of both arms (the same string, so the lines compare)."""
+    return f"c2c {n}^3 complex<{'float' if prec == 0 else 'double'}> fwd(scale::full)+bwd"
+
+
 def flops_per_transform(n_total):
     return 5.0 * n_total * math.log2(n_total)
 
@@ -148,8 +153,7 @@ def reference_arm(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64" if prec == 0 else "c128", "data": "synthetic",
-        "config": {"workload": f"c2c {args.size}^3 complex<{'float' if prec == 0 else 'double'}> fwd(scale::full)+bwd",
-                   "global_batch": 1, "parallelism": "host threads"},
+        "config": {"workload": workload_string(args.size, prec), "global_batch": 1, "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} x (forward+backward) of the full {args.size}^3 box, "
                                    f"C restatement of the heFFTe stock backend, {threads} OpenMP threads"},
@@ -326,24 +330,32 @@ def ours(args, rank, world, local_rank):
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         cv, csec = cpu_run(n, prec, 1, 0, threads)
+        # single-core latency: the reference's stock backend is single-threaded
+        sv, ssec = cpu_run(n, prec, 1, 0, 1)
         cpu = {"value": cv, "unit": "GFLOP/s", "cores": threads, "kind": "port",
                "sample": f"1 x (forward+backward) of the full {n}^3 box, C restatement of the heFFTe stock "
-                         f"backend, {threads} OpenMP threads ({csec:.2f} s)"}
+                         f"backend, {threads} OpenMP threads ({csec:.2f} s)",
+               "single_core": {"value": sv, "unit": "GFLOP/s", "cores": 1, "ms_per_step": ssec * 1e3,
+                               "sample": f"1 x (forward+backward) of the full {n}^3 box on one thread "
+                                         f"({ssec:.2f} s)"}}
     line = {
         "metric": metric_name(),
         "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64" if prec == 0 else "c128", "data": "synthetic",
-        "config": {"workload": f"c2c {n}^3 complex<{'float' if prec == 0 else 'double'}> fwd(scale::full)+bwd, "
-                               "out of place, caller workspace",
+        "config": {"workload": workload_string(n, prec), "placement": "out of place, caller workspace",
                    "global_batch": world, "parallelism": f"replicas x{world}",
                    "l2": f"inputs {N * esize / 2**30:.2f} GiB > 129 MB L2 (no flush needed)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "peak_nominal": NOMINAL_HBM_GBS, "frac_nominal": achieved / NOMINAL_HBM_GBS,
-                     # DRAM read+write bytes per launch of the column pass kernel, from the ncu
-                     # launch list of this command (profiles/k_pipe_c2c_512cube_fp32.md)
+                     # DRAM read+write bytes per launch of the column pass kernel: not measured
+                     # in this run, but taken from one ncu capture of this command
+                     # (profiles/k_pipe_c2c_512cube_fp32.md); traffic_source says so in the line
                      "traffic": 2.083e9 if (n == 512 and prec == 0) else None,
+                     "traffic_source": ("ncu capture of this command (dram__bytes_read.sum + "
+                                        "dram__bytes_write.sum per launch), profiles/k_pipe_c2c_512cube_fp32.md; "
+                                        "not measured in this run") if (n == 512 and prec == 0) else None,
                      "kernel": "k_pipe " + ("column" if dom else "line") + f" pass along dim {dom}",
                      "algorithmic_bytes_per_launch": pass_bytes,
                      "per_pass_ms": {str(d): per_launch[d] for d in per_launch},
@@ -366,29 +378,57 @@ def ours(args, rank, world, local_rank):
 NOMINAL_HBM_GBS = 7900.0   # GB300 HBM3e nominal bandwidth
 
 
-def fp64_check(gb, box, x, stream, forms, kind="c2c"):
-    """rel-L2 of the forward transform of x by each plan in `forms` against this
-    library's double-precision transform of the same input (the FP64 path the
-    parity tests hold to 1e-12 of the FP64 oracle); kind c2c, r2c or cos."""
-    import torch
+def fp64_host(kind, size, x, y=None, conv=False):
+    """FP64 result for the input x (a device tensor of the box in order
+    (0, 1, 2)), computed on the host by pocketfft (scipy.fft, all host
+    threads) with heFFTe's conventions: the unscaled forward transform of kind
+    c2c, r2c (along dimension 0) or cos (DCT-II = REDFT10 along every
+    dimension, scipy's type-2 DCT); conv: the circular convolution of x and y
+    (y None: x with itself), i.e. backward(forward(x) .* forward(y)) with
+    scale::full.  Outside every timed region."""
+    import scipy.fft as sf
+    w = os.cpu_count() or 1
+    shape = (size[2], size[1], size[0])       # numpy axes: dimension 2, 1, 0
+
+    def host(t, dt):
+        return t.cpu().numpy().reshape(shape).astype(dt)
+    if conv:
+        if kind == "r2c":
+            fx = sf.rfftn(host(x, np.float64), workers=w)
+            fy = fx if y is None else sf.rfftn(host(y, np.float64), workers=w)
+            return sf.irfftn(fx * fy, s=shape, workers=w)
+        fx = sf.fftn(host(x, np.complex128), workers=w)
+        fy = fx if y is None else sf.fftn(host(y, np.complex128), workers=w)
+        return sf.ifftn(fx * fy, workers=w)
     if kind == "c2c":
-        p64 = gb.fft3d(box, box, stream=stream)
-        x64 = x.to(torch.complex128)
-    elif kind == "r2c":
-        p64 = gb.fft3d_r2c(box, box.r2c(0), 0, stream=stream)
-        x64 = x.to(torch.float64)
-    else:
-        p64 = gb.rtransform(gb.kind.cos, box, box, stream=stream)
-        x64 = x.to(torch.float64)
-    odt = torch.complex128 if kind != "cos" else torch.float64
-    y64 = torch.empty(p64.size_outbox(), dtype=odt, device=x.device)
-    p64.forward(x64, y64)
-    del x64
+        return sf.fftn(host(x, np.complex128), workers=w)
+    if kind == "r2c":
+        return sf.rfftn(host(x, np.float64), workers=w)
+    return sf.dctn(host(x, np.float64), type=2, workers=w)
+
+
+def rel_l2_host(got, ref, chunk=1 << 24):
+    """||got - ref|| / ||ref|| in float64 (got: device tensor), in chunks."""
+    g = got.cpu().numpy().ravel()
+    r = np.asarray(ref).ravel()
+    num = den = 0.0
+    for i in range(0, r.size, chunk):
+        gi, ri = g[i:i + chunk].astype(r.dtype), r[i:i + chunk]
+        num += float(np.sum(np.abs(gi - ri) ** 2))
+        den += float(np.sum(np.abs(ri) ** 2))
+    return float(np.sqrt(num / den))
+
+
+def fp64_check(gb, box, x, stream, forms, kind="c2c"):
+    """rel-L2 of the forward transform of x by each plan in `forms` against
+    the host FP64 transform of the same input (fp64_host)."""
+    import torch
+    ref = fp64_host(kind, box.size, x)
     out = {}
     for name, p in forms.items():
         y = torch.empty(p.size_outbox(), dtype=torch.complex64 if kind != "cos" else torch.float32, device=x.device)
         p.forward(x, y)
-        out[name] = float((torch.linalg.vector_norm(y.to(odt) - y64) / torch.linalg.vector_norm(y64)).item())
+        out[name] = rel_l2_host(y, ref)
         del y
     return out
 
@@ -424,7 +464,8 @@ def tensor_core_form(gb, box, x, y, z, work, stream, args, ms_fp32, world):
             "value": world * 2 * flops_per_transform(n_total) / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
             "ms_per_step": ms, "speedup_vs_fp32": ms_fp32 / ms,
             "step_gbs": step_bytes / (ms / 1e3) / 1e9, "step_frac": step_bytes / (ms / 1e3) / 1e9 / peak,
-            "rel_l2_forward_vs_fp64": acc["tensor_cores"], "rel_l2_forward_vs_fp64_plain_fp32": acc["fp32"]}
+            "rel_l2_forward_vs_fp64": acc["tensor_cores"], "rel_l2_forward_vs_fp64_plain_fp32": acc["fp32"],
+            "fp64_reference": "pocketfft FP64 (scipy.fft) of the same input on the host"}
 
 
 WORKLOADS = {
@@ -611,9 +652,8 @@ def run_selector_workload(name):
 def run_conv_workload(name, steps, warmup):
     """plan.convolve on a c2c (or r2c) box: time per convolution, GFLOP/s
     counting its transforms (5 N log2 N each: 2 for x .* x, 3 for x .* y), the
-    bytes of its passes against the HBM peak, and the result against this
-    library's double-precision convolution of the same input (the FP64 path
-    the parity tests hold to 1e-12 of the FP64 oracle)."""
+    bytes of its passes against the HBM peak, and the result against the host
+    FP64 convolution of the same input (fp64_host)."""
     import torch
     import heffte_gb300 as gb
     _, size, prec, form = WORKLOADS[name]
@@ -677,12 +717,7 @@ def run_conv_workload(name, steps, warmup):
         b = units * N * cs
     peak, _ = peaks()
     del work
-    hdt = torch.float64 if real else torch.complex128
-    x64 = x.to(hdt)
-    y64 = y.to(hdt) if two else None
-    o64 = torch.empty_like(x64)
-    make_plan().convolve(x64, y64, o64, gb.scale.full)
-    err = float((torch.linalg.vector_norm(out.to(hdt) - o64) / torch.linalg.vector_norm(o64)).item())
+    err = rel_l2_host(out, fp64_host("r2c" if real else "c2c", size, x, y, conv=True))
     return {"workload": name, "form": form, "fused_dim": route, "ms_per_step": ms,
             "gflops": ntrans * flops_per_transform(N) / (ms / 1e3) / 1e9,
             "bytes_per_step": b, "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak,

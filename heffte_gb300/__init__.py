@@ -91,6 +91,9 @@ def lib():
     for f in ("input_size", "output_size", "workspace_size"):
         getattr(L, "heffte_gb300_boxbatch_" + f).argtypes = [vp]
         getattr(L, "heffte_gb300_boxbatch_" + f).restype = ll
+    L.heffte_gb300_set_dependency_wait_budget.argtypes = [ll]
+    L.heffte_gb300_dependency_wait_budget.restype = ll
+    L.heffte_gb300_boxbatch_hold_dependencies.argtypes = [vp, i]
     L.heffte_gb300_boxbatch_forward.argtypes = [vp, vp, vp, i]
     L.heffte_gb300_boxbatch_backward.argtypes = [vp, vp, vp, vp, i]
     L.heffte_gb300_tune.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_int)]
@@ -420,10 +423,22 @@ def set_kernel_variant(variant):
 
 
 def device_status(reset=False):
-    """Status word of the current device (0 = no kernel gave up a bounded wait)."""
+    """Status word of the current device: 0 = no kernel gave up a bounded wait;
+    1 a bulk-copy wait, 2 a batch pass-dependency wait, 3 a tensor-core MMA wait."""
     v = ctypes.c_int(-1)
     check(lib().heffte_gb300_device_status(ctypes.byref(v), int(reset)))
     return v.value
+
+
+DEV_TIMEOUT_BULK_COPY, DEV_TIMEOUT_DEPENDENCY, DEV_TIMEOUT_MMA = 1, 2, 3
+
+
+def set_dependency_wait_budget(clocks):
+    """Clock budget of the batch kernel's waits for another CTA's pass of the
+    same box (default 4e9); returns the previous budget."""
+    old = lib().heffte_gb300_dependency_wait_budget()
+    check(lib().heffte_gb300_set_dependency_wait_budget(int(clocks)))
+    return old
 
 
 class boxbatch:
@@ -457,6 +472,11 @@ class boxbatch:
 
     def workspace_size(self):
         return lib().heffte_gb300_boxbatch_workspace_size(self._h)
+
+    def hold_dependencies(self, hold):
+        """Test hook: every pass dependency waits for a tile that never comes
+        (hold=True), so the waits run out of their budget; False restores."""
+        check(lib().heffte_gb300_boxbatch_hold_dependencies(self._h, int(bool(hold))))
 
     def forward(self, inarray, outarray, scaling=scale.none):
         check(lib().heffte_gb300_boxbatch_forward(self._h, _ptr(inarray), _ptr(outarray), scaling))

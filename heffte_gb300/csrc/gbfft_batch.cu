@@ -15,6 +15,7 @@
 #include "gbfft_batch.h"
 #include "gbfft_kernels.cuh"
 #include "gbfft_ptx.cuh"
+#include <atomic>
 #include <numeric>
 
 namespace gbfft {
@@ -26,6 +27,7 @@ struct BatchUnit {
     int tpb;             // transforms (or pairs) per tile
     int src, dst;        // buffers: 0 input, 1 output, 2 workspace
     int dep;             // unit that must complete first (-1: none)
+    int dep_extra;       // tiles awaited beyond the dependency's own (0; 1 only under hold_dependencies)
     int last;            // carries the scale
     long long G;         // transforms of this pass
     long long tiles, tile0;
@@ -34,7 +36,6 @@ struct BatchUnit {
     double scale;
 };
 
-enum { DEV_TIMEOUT_DEPENDENCY = 2 };
 // CTAs per SM the batch kernels are compiled for (registers per thread
 // <= 65536 / (256 x this)); float measured best at 4, double kept at 2
 template<typename T> constexpr int batch_ctas_per_sm(){ return sizeof(T) == 4 ? 4 : 2; }
@@ -51,7 +52,7 @@ template<typename T, bool FWD>
 __global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
-        long long total_tiles, int *status, int scaling){
+        long long total_tiles, int *status, int scaling, long long dep_budget){
     using C = c_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
     C *sm = reinterpret_cast<C*>(smraw);
@@ -93,12 +94,12 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
         BatchUnit const &U = units[u];
         bool ok = true;
         if (tid == 0 && U.dep >= 0){
-            long long need = units[U.dep].tiles;
+            long long need = units[U.dep].tiles + U.dep_extra;
             volatile int *d = done + U.dep;
             if (*d < need){
                 long long t0 = clock64();
                 while (*d < need){
-                    if (clock64() - t0 > 4000000000LL){ atomicExch(status, DEV_TIMEOUT_DEPENDENCY); ok = false; break; }
+                    if (clock64() - t0 > dep_budget){ atomicExch(status, DEV_TIMEOUT_DEPENDENCY); ok = false; break; }
                 }
             }
             __threadfence();
@@ -150,6 +151,25 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
 // host side
 // ---------------------------------------------------------------------------
 static constexpr int kBatchThreads = 256;
+
+static std::atomic<long long> g_dep_budget{kWaitBudgetClocks};
+long long dependency_wait_budget(){ return g_dep_budget.load(); }
+void set_dependency_wait_budget(long long clocks){
+    if (clocks < 0) throw Error(ST_INVALID, "the wait budget must be >= 0 clocks");
+    g_dep_budget.store(clocks);
+}
+
+// Test hook: every pass dependency waits for one tile more than its pass has
+// (hold = true), so each such wait runs out of its budget; hold = false
+// restores the tables.
+void Batch::hold_dependencies(bool hold){
+    for (int dir = 0; dir < 2; dir++){
+        std::vector<BatchUnit> &u = dir == 0 ? h_fwd_units : h_bwd_units;
+        for (auto &U : u) U.dep_extra = (hold && U.dep >= 0) ? 1 : 0;
+        check_cuda(cudaMemcpy(dir == 0 ? d_fwd_units : d_bwd_units, u.data(), u.size() * sizeof(BatchUnit),
+                              cudaMemcpyHostToDevice), "copy units");
+    }
+}
 
 Batch::~Batch(){
     if (fwd_exec) cudaGraphExecDestroy(fwd_exec);
@@ -306,6 +326,8 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         }
     }
     b->nunits = (int)fu.size();
+    b->h_fwd_units = fu;
+    b->h_bwd_units = bu;
     // device tables
     auto dalloc = [&](size_t bytes) -> void* {
         void *p = nullptr;
@@ -365,8 +387,9 @@ static void build_graph(Batch &b, bool fwd){
     b.args_total = fwd ? b.fwd_tiles : b.bwd_tiles;
     b.args_status = device_status();
     b.args_scaling = 0;
+    b.args_budget = dependency_wait_budget();
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
-                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling};
+                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget};
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(batch_kernel(b.prec, fwd));
     kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
@@ -395,8 +418,9 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     args_total = fwd ? fwd_tiles : bwd_tiles;
     args_status = device_status();
     args_scaling = scaling;
+    args_budget = dependency_wait_budget();
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
-                    &args_total, &args_status, &args_scaling};
+                    &args_total, &args_status, &args_scaling, &args_budget};
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(batch_kernel(prec, fwd));
     kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));

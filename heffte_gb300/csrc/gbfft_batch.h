@@ -33,6 +33,7 @@ std::string device_key();
 // batch of boxes (gbfft_batch.cu)
 // ---------------------------------------------------------------------------
 struct BatchBufs { void const *in; void *out; void *work; };
+struct BatchUnit;   // one 1-D pass of one box (gbfft_batch.cu)
 
 struct Batch {
     int kind = PK_R2C;
@@ -62,10 +63,19 @@ struct Batch {
     long long args_total = 0;
     int *args_status = nullptr;
     int args_scaling = 0;
+    long long args_budget = 0;
+    // host copies of the unit tables (their layout is private to gbfft_batch.cu)
+    std::vector<BatchUnit> h_fwd_units, h_bwd_units;
     ~Batch();
+    void hold_dependencies(bool hold);
     long long workspace_elems() const { return out_total; }
     void run(bool fwd, void const *in, void *out, void *work, int scaling);
 };
+
+// Clock budget of the batch kernel's waits for another CTA's pass of the same
+// box (default kWaitBudgetClocks); read at every launch.
+long long dependency_wait_budget();
+void set_dependency_wait_budget(long long clocks);
 
 std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream);
 

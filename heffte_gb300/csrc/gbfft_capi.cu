@@ -108,6 +108,7 @@ static int pack_common(void *stream, int dtype, long long nf, long long nm, long
         check_sizes(nf, nm, ns);
         if (nf == 0 || nm == 0 || ns == 0) return;
         if (!src || !dst) throw Error(ST_INVALID, "null pointer");
+        strided_extent(nf, nm, ns, ls, ps, pack ? "direct_pack source" : "direct_unpack destination");
         launch_direct_pack(as_stream(stream), dtype, nf, nm, ns, ls, ps, src, dst, pack);
         check_cuda(cudaPeekAtLastError(), pack ? "direct_pack kernel launch" : "direct_unpack kernel launch");
     });
@@ -133,6 +134,11 @@ int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long
         if (!valid_order({map0, map1, map2})) throw Error(ST_INVALID, "map must be a permutation of 0, 1, 2");
         if (nfast == 0 || nmid == 0 || nslow == 0) return;
         if (!src || !dst) throw Error(ST_INVALID, "null pointer");
+        // the source's a-th dimension (fast, mid, slow) is destination dimension map[a]
+        long long size[3] = {nfast, nmid, nslow};
+        strided_extent(nfast, nmid, nslow, line_stride, plane_stride, "transpose_unpack destination");
+        strided_extent(size[map0], size[map1], size[map2], buff_line_stride, buff_plane_stride,
+                       "transpose_unpack source");
         launch_transpose_unpack(as_stream(stream), dtype, nfast, nmid, nslow, line_stride, plane_stride,
                                 buff_line_stride, buff_plane_stride, map0, map1, src, dst);
         check_cuda(cudaPeekAtLastError(), "transpose_unpack kernel launch");
@@ -342,6 +348,19 @@ int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch b, const void *input, v
         if (!b) throw Error(ST_INVALID, "null batch");
         b->b->run(false, input, output, workspace, scale);
         check_cuda(cudaPeekAtLastError(), "batched backward transform");
+    });
+}
+
+int heffte_gb300_set_dependency_wait_budget(long long clocks){
+    return guard([&]{ set_dependency_wait_budget(clocks); });
+}
+
+long long heffte_gb300_dependency_wait_budget(void){ return dependency_wait_budget(); }
+
+int heffte_gb300_boxbatch_hold_dependencies(heffte_gb300_boxbatch b, int hold){
+    return guard([&]{
+        if (!b) throw Error(ST_INVALID, "null batch");
+        b->b->hold_dependencies(hold != 0);
     });
 }
 

@@ -86,6 +86,12 @@ void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout 
                 void *out, long long G, double scale, LaunchCfg cfg = {});
 
 // Location-layer data movement.
+// Validates a strided 3-D layout of n0 x n1 x n2 elements (n0 fastest, line
+// stride ls, plane stride ps): strides non-negative, lines and planes that do
+// not overlap, and a span that fits in 63 bits.  Returns the number of
+// elements the layout spans ((n2-1) ps + (n1-1) ls + n0); throws ST_INVALID
+// naming `what` otherwise.  All sizes must be positive.
+long long strided_extent(long long n0, long long n1, long long n2, long long ls, long long ps, char const *what);
 void launch_direct_pack(cudaStream_t s, int dtype, long long nf, long long nm, long long ns, long long ls,
                         long long ps, void const *src, void *dst, bool pack);
 void launch_transpose_unpack(cudaStream_t s, int dtype, long long nf, long long nm, long long ns, long long ls,

@@ -12,13 +12,15 @@
 // a fixed size (kNoAllocScratchBytes below).  Every GPU that loads the library
 // reserves that array until the process exits.  The device address of the
 // array is looked up once per device, on the first call made while that
-// device is current; make that first call before any stream capture begins.
+// device is current (and again on the first call after cudaDeviceReset made a
+// new context); make that first call before any stream capture begins.
 // All calls share the array and it keeps the last call's contents; calls
 // whose work overlaps on the GPU (for example on two streams) race on it.
 // The copy into the array and the transpose are enqueued on the caller's
 // stream; nothing here calls cudaMalloc, cudaFree or an allocating library.
 #include "gbfft_plan.h"
 #include "../../include/heffte_gb300.h"
+#include <cuda.h>
 
 namespace gbfft {
 namespace {
@@ -27,21 +29,56 @@ constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;   // 32 MiB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of the scratch array for the current device (looked up once
-// per device with that device current; the host-side symbol is only a handle).
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (no
+// link dependency on libcuda); null when the driver does not offer them.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+template<typename F>
+F driver_fn(char const *name){
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess){
+        cudaGetLastError();
+        return nullptr;
+    }
+    return reinterpret_cast<F>(p);
+}
+
+// Unique id of the current context (0 when it cannot be read).  A context
+// made after cudaDeviceReset gets a new id, so the cached address below is
+// looked up again rather than reused.
+unsigned long long current_context_id(){
+    static CtxGetCurrentFn get_ctx = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+    static CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_ctx || !get_id || get_ctx(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array for the current device.  The host-side
+// symbol is only a handle, so the address is looked up with
+// cudaGetSymbolAddress once per device (and context), with that device current.
 void *noalloc_scratch(){
-    static void *ptrs[64] = {nullptr};
+    struct Entry { void *ptr; unsigned long long ctx; };
+    static Entry cache[64] = {};
     static std::mutex mu;
     int dev = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= 64) throw Error(ST_UNSUPPORTED, "device index out of range for the no-allocation scratch table");
+    unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lk(mu);
-    if (!ptrs[dev]){
+    Entry &e = cache[dev];
+    if (!e.ptr || e.ctx != ctx){
         void *p = nullptr;
         check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-allocation scratch)");
-        ptrs[dev] = p;
+        e.ptr = p;
+        // the lookup makes the context if there was none yet: key on its id now
+        e.ctx = current_context_id();
     }
-    return ptrs[dev];
+    return e.ptr;
 }
 
 } // namespace
@@ -65,13 +102,19 @@ extern "C" int heffte_gb300_transpose_unpack_inplace_noalloc(void *stream, int d
         }
         if (!data) throw Error(ST_INVALID, "null pointer");
         // the source occupies the buffer in its own layout: its a-th dimension
-        // (fast, mid, slow) is the destination dimension map[a]
+        // (fast, mid, slow) is the destination dimension map[a]; both layouts
+        // are checked (non-negative, non-overlapping strides, no overflow)
+        // before the span of the source is compared with the scratch size
         long long size[3] = {nfast, nmid, nslow};
-        long long extent = (size[m[2]] - 1) * buff_plane_stride + (size[m[1]] - 1) * buff_line_stride + size[m[0]];
-        size_t bytes = (size_t)extent * (size_t)elem_size(dtype);
-        if (bytes > kNoAllocScratchBytes)
-            throw Error(ST_INVALID, "the source of " + std::to_string(bytes) + " bytes exceeds the " +
-                        std::to_string(kNoAllocScratchBytes >> 20) + " MiB scratch of the no-allocation transpose");
+        strided_extent(nfast, nmid, nslow, line_stride, plane_stride, "destination");
+        long long extent = strided_extent(size[m[0]], size[m[1]], size[m[2]], buff_line_stride, buff_plane_stride,
+                                          "source");
+        long long es = elem_size(dtype);
+        if (extent > (long long)(kNoAllocScratchBytes / (size_t)es))
+            throw Error(ST_INVALID, "the source of " + std::to_string(extent) + " elements of " + std::to_string(es) +
+                        " bytes exceeds the " + std::to_string(kNoAllocScratchBytes >> 20) +
+                        " MiB scratch of the no-allocation transpose");
+        size_t bytes = (size_t)extent * (size_t)es;
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
         void *scratch = noalloc_scratch();
         check_cuda(cudaMemcpyAsync(scratch, data, bytes, cudaMemcpyDeviceToDevice, s), "copy into no-allocation scratch");

@@ -152,6 +152,20 @@ int elem_size(int dtype){
     }
 }
 
+long long strided_extent(long long n0, long long n1, long long n2, long long ls, long long ps, char const *what){
+    auto bad = [&](std::string const &why){ return Error(ST_INVALID, std::string(what) + " layout: " + why); };
+    if (ls < 0 || ps < 0) throw bad("negative stride");
+    // a line must not run into the next one, a plane not into the next plane
+    if (n1 > 1 && ls < n0) throw bad("line stride " + std::to_string(ls) + " below the line length " + std::to_string(n0));
+    long long plane = 0, span = 0, t = 0;
+    if (__builtin_mul_overflow(n1 - 1, ls, &t) || __builtin_add_overflow(t, n0, &plane))
+        throw bad("size overflow");
+    if (n2 > 1 && ps < plane) throw bad("plane stride " + std::to_string(ps) + " below the plane extent " + std::to_string(plane));
+    if (__builtin_mul_overflow(n2 - 1, ps, &t) || __builtin_add_overflow(t, plane, &span))
+        throw bad("size overflow");
+    return span;
+}
+
 void launch_direct_pack(cudaStream_t s, int dtype, long long nf, long long nm, long long ns, long long ls, long long ps,
                         void const *src, void *dst, bool pack){
     int es = elem_size(dtype);

@@ -8,7 +8,15 @@
 namespace gbfft {
 
 // status codes written by kernels into the device status word
-enum { DEV_OK = 0, DEV_TIMEOUT_BULK_COPY = 1 };
+enum { DEV_OK = 0, DEV_TIMEOUT_BULK_COPY = 1, DEV_TIMEOUT_DEPENDENCY = 2, DEV_TIMEOUT_MMA = 3 };
+
+// Default clock budget of every bounded wait (about two seconds at 2 GHz).
+// The waits for bulk copies and for tensor-core MMAs keep it: a CTA that gave
+// up on them early would return while a copy or an MMA may still write its
+// shared or tensor memory.  The batch kernel's wait for another CTA's pass of
+// the same box has nothing of its own in flight, so its budget is a launch
+// argument that can be shortened (heffte_gb300_set_dependency_wait_budget).
+constexpr long long kWaitBudgetClocks = 4000000000LL;
 
 __device__ __forceinline__ uint32_t smem_u32(void const *p){
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -45,7 +53,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity){
 // Waits for phase `parity` of the barrier; gives up after ~`budget` clocks,
 // records DEV_TIMEOUT_BULK_COPY in *status and returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status,
-                                                  long long budget = 4000000000LL){
+                                                  long long budget = kWaitBudgetClocks){
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
     while (true){

@@ -50,8 +50,6 @@
 
 namespace gbfft {
 
-enum { DEV_TIMEOUT_MMA = 3 };
-
 namespace {
 
 // ---------------------------------------------------------------------------
@@ -189,7 +187,7 @@ __device__ __forceinline__ bool mma_wait(uint64_t *bar, uint32_t parity, int *st
     long long t0 = clock64();
     while (true){
         if (mbar_try_wait(bar, parity)) return true;
-        if (clock64() - t0 > 4000000000LL){
+        if (clock64() - t0 > kWaitBudgetClocks){
             if (status) atomicExch(status, DEV_TIMEOUT_MMA);
             return false;
         }

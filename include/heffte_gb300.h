@@ -68,9 +68,11 @@ int heffte_gb300_version(void);
  * kernels only, 2 pipelined kernels wherever they apply. */
 int heffte_gb300_set_kernel_variant(int variant);
 
-/* No reference counterpart.  Reads the current device's status word (0 = no
- * fault; 1 = a bounded wait for a bulk copy gave up and the kernel returned
- * early, its output is invalid).  Synchronises with the device.  reset != 0
+/* No reference counterpart.  Reads the current device's status word: 0 = no
+ * fault; otherwise a bounded device wait gave up and its kernel returned
+ * early, so that call's output is invalid: 1 = a wait for a bulk (TMA) copy,
+ * 2 = the batch kernel's wait for another CTA's pass of the same box, 3 = a
+ * wait for tensor-core MMAs.  Synchronises with the device.  reset != 0
  * clears the word after reading. */
 int heffte_gb300_device_status(int *status, int reset);
 
@@ -102,7 +104,9 @@ int heffte_gb300_direct_unpack(void *stream, int dtype, long long nfast, long lo
 /* Replaces cuda::transpose_unpack (src/heffte_backend_cuda.cu:404-441), i.e.
  * transpose_packer<tag::gpu>::unpack (include/heffte_backend_cuda.h:824-828):
  * dst[k*plane_stride + j*line_stride + i] = src[<map case>] for the six
- * (map0, map1, map2) cases of the reference kernel (:90-133). Bit-exact. */
+ * (map0, map1, map2) cases of the reference kernel (:90-133). Bit-exact.
+ * Strides that are negative or make lines / planes overlap, on either side,
+ * are rejected with HEFFTE_GB300_INVALID (also for direct_pack / unpack). */
 int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long long nmid, long long nslow,
                                   long long line_stride, long long plane_stride,
                                   long long buff_line_stride, long long buff_plane_stride,
@@ -117,9 +121,10 @@ int heffte_gb300_transpose_unpack(void *stream, int dtype, long long nfast, long
  * destination (line_stride, plane_stride); the six maps are those of
  * heffte_gb300_transpose_unpack.  The source is staged in a fixed 32 MiB
  * scratch array inside the library (reserved on every GPU that loads the
- * library until the process exits); a larger source is rejected with
- * HEFFTE_GB300_INVALID.  The first call on a device looks up the array's
- * device address; make it before any stream capture.  All calls share the
+ * library until the process exits); a larger source, and strides that are
+ * negative, overlap or overflow, are rejected with HEFFTE_GB300_INVALID.  The
+ * first call on a device (and the first after a cudaDeviceReset) looks up the
+ * array's device address; make it before any stream capture.  All calls share the
  * array, which keeps the last call's contents, so calls that overlap on the
  * GPU (e.g. on two streams) race.  Nothing is allocated. */
 int heffte_gb300_transpose_unpack_inplace_noalloc(void *stream, int dtype, long long nfast, long long nmid,
@@ -276,6 +281,21 @@ long long heffte_gb300_boxbatch_workspace_size(heffte_gb300_boxbatch batch);
 int heffte_gb300_boxbatch_forward(heffte_gb300_boxbatch batch, const void *input, void *output, int scale);
 int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *input, void *output, void *workspace,
                                    int scale);
+
+/* No reference counterpart.  Clock budget (GPU clocks, >= 0) after which the
+ * batch kernel's wait for another CTA's pass of the same box gives up, records
+ * status 2 (heffte_gb300_device_status) and returns; read at every batch
+ * launch; default 4e9 (about two seconds).  The waits for bulk copies and
+ * tensor-core MMAs keep the default: giving up on them early could return
+ * while a copy or an MMA still writes the CTA's memory. */
+int heffte_gb300_set_dependency_wait_budget(long long clocks);
+long long heffte_gb300_dependency_wait_budget(void);
+/* No reference counterpart; a test hook for the give-up path.  hold = 1 makes
+ * every pass dependency of the batch wait for one tile more than its pass has
+ * (a count no CTA reaches), so each such wait runs out of its budget; hold = 0
+ * restores the batch.  Nothing faults: the waiting CTAs record status 2 and
+ * return. */
+int heffte_gb300_boxbatch_hold_dependencies(heffte_gb300_boxbatch batch, int hold);
 
 /* No reference counterpart.  Measures, on the current device, every candidate
  * radix plan and tile size of each length and keeps the fastest for later

@@ -41,3 +41,20 @@ def gb():
         build.build()
     heffte_gb300.lib()
     return heffte_gb300
+
+
+_REPORT = []
+
+
+@pytest.fixture(scope="session")
+def report():
+    """Collects lines (e.g. measured errors) printed at the end of the run,
+    also under -q."""
+    return _REPORT
+
+
+def pytest_terminal_summary(terminalreporter):
+    if _REPORT:
+        terminalreporter.section("measured")
+        for line in _REPORT:
+            terminalreporter.write_line(line)

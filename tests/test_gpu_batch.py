@@ -94,3 +94,40 @@ def test_tuner_resumes_from_cache_and_batch_uses_tuned_plans(gb):
         xi = x[b.input_offset(i):b.input_offset(i) + n]
         assert O.rel_l2(yh[b.output_offset(i):b.output_offset(i) + nc], O.fft3d_r2c(xi, s, 0)) < 1e-6
     gb.tune_clear()
+
+
+def test_dependency_wait_gives_up_and_the_next_call_is_correct(gb):
+    """The give-up path of the batch kernel's bounded pass-dependency wait.
+
+    With the dependencies held (each waits for one tile more than its pass
+    has, a count no CTA reaches) and a 2e6-clock budget (about a millisecond),
+    every waiting CTA must give up, record status 2, and return; the launch
+    then ends by itself.  After the status is read and cleared, the budget
+    restored and the hold lifted, the same batch must run correctly."""
+    rng = np.random.default_rng(99)
+    sizes = _sizes(rng, 24, SIDES[:6])
+    b = gb.boxbatch(gb.kind.r2c, sizes, 0)
+    x = rng.standard_normal(b.input_size()).astype(np.float32)
+    xin = torch.from_numpy(x).cuda()
+    y = torch.zeros(b.output_size(), dtype=torch.complex64, device="cuda")
+    assert gb.device_status(reset=True) == 0
+    old = gb.set_dependency_wait_budget(2_000_000)
+    try:
+        b.hold_dependencies(True)
+        b.forward(xin, y)
+        torch.cuda.synchronize()
+        assert gb.device_status(reset=True) == gb.DEV_TIMEOUT_DEPENDENCY
+    finally:
+        gb.set_dependency_wait_budget(old)
+        b.hold_dependencies(False)
+    assert old == 4_000_000_000
+    assert gb.device_status() == 0
+    b.forward(xin, y)
+    yh = y.cpu().numpy()
+    for i, s in enumerate(sizes):
+        n = int(np.prod(s))
+        nc = (s[0] // 2 + 1) * s[1] * s[2]
+        xi = x[b.input_offset(i):b.input_offset(i) + n]
+        yi = yh[b.output_offset(i):b.output_offset(i) + nc]
+        assert O.rel_l2(yi, O.fft3d_r2c(xi, s, 0)) < TOL[0], (i, s)
+    assert gb.device_status() == 0

@@ -17,7 +17,8 @@ import tempfile
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+# the reference heFFTe tree: $HEFFTE_REFERENCE_DIR, else "reference" beside this repository
+REF = os.environ.get("HEFFTE_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 CUDA = "/usr/local/cuda"
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")) or shutil.which("g++") is None,

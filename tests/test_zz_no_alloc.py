@@ -26,13 +26,17 @@ def _bind(L):
     return L
 
 
-def _case(L, rng, dtype, size, mp):
+def _case(L, rng, dtype, size, mp, pad=(0, 0)):
+    """pad = extra elements per source line and per source plane (a padded
+    buffer layout, whose span differs from its element count)."""
     nf, nm, ns = size
     src_dims = [size[mp[a]] for a in range(3)]
-    bls, bps = src_dims[0], src_dims[0] * src_dims[1]
+    bls = src_dims[0] + pad[0]
+    bps = bls * src_dims[1] + pad[1]
     ls, ps = nf, nf * nm
     es = ESIZE[dtype]
-    n = max(int(np.prod(src_dims)), ns * ps)
+    src_span = (src_dims[2] - 1) * bps + (src_dims[1] - 1) * bls + src_dims[0]
+    n = max(src_span, ns * ps)
     host = rng.integers(0, 256, n * es, dtype=np.uint8)
     data = torch.from_numpy(host).cuda()
     src_copy = data.clone()
@@ -52,10 +56,14 @@ def test_noalloc_inplace_transpose_matches_allocating_path(gb):
     L = _bind(gb.lib())
     rng = np.random.default_rng(2024)
     # two calls in a row, different shapes, maps and element types
-    for dtype, size, mp in [(2, (67, 45, 33), (2, 0, 1)), (3, (40, 28, 19), (1, 2, 0)),
-                            (0, (129, 31, 17), (2, 1, 0))]:
-        got, want = _case(L, rng, dtype, size, mp)
-        assert got.tobytes() == want.tobytes(), (dtype, size, mp)
+    for dtype, size, mp, pad in [(2, (67, 45, 33), (2, 0, 1), (0, 0)), (3, (40, 28, 19), (1, 2, 0), (0, 0)),
+                                 (0, (129, 31, 17), (2, 1, 0), (0, 0)),
+                                 # map0 == 0: the row-copy branch (source rows stay rows)
+                                 (1, (70, 23, 41), (0, 2, 1), (0, 0)),
+                                 # padded source lines and planes
+                                 (2, (37, 52, 29), (1, 0, 2), (5, 17)), (3, (33, 18, 27), (0, 2, 1), (3, 0))]:
+        got, want = _case(L, rng, dtype, size, mp, pad)
+        assert got.tobytes() == want.tobytes(), (dtype, size, mp, pad)
 
 
 def test_noalloc_rejects_oversized_source(gb):
@@ -66,3 +74,22 @@ def test_noalloc_rejects_oversized_source(gb):
                                                          1, 0, 2, t.data_ptr())
     assert rc == 1
     assert b"MiB scratch" in L.heffte_gb300_last_error()
+
+
+def test_noalloc_rejects_inconsistent_strides(gb):
+    """Negative, overlapping or overflowing strides are refused before any copy
+    (a wrapped span could otherwise pass the scratch-size check)."""
+    L = _bind(gb.lib())
+    t = torch.zeros(64, dtype=torch.float32, device="cuda")
+    bad = [
+        (8, 4, 2, 8, 32, -8, 32),           # negative source line stride
+        (8, 4, 2, 8, 32, 8, -32),           # negative source plane stride
+        (8, 4, 2, 8, 32, 3, 32),            # source lines overlap
+        (8, 4, 2, 4, 32, 8, 32),            # destination lines overlap
+        (8, 4, 2, 8, 32, 8, 1 << 62),       # span overflows 63 bits
+    ]
+    for nf, nm, ns, ls, ps, bls, bps in bad:
+        rc = L.heffte_gb300_transpose_unpack_inplace_noalloc(None, 0, nf, nm, ns, ls, ps, bls, bps, 0, 1, 2,
+                                                             t.data_ptr())
+        assert rc == 1, (nf, nm, ns, ls, ps, bls, bps)
+        assert b"layout" in L.heffte_gb300_last_error()
