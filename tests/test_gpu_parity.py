@@ -168,6 +168,41 @@ def test_executor_each_dimension(gb, order, prec):
     assert O.rel_l2(host(t), O.fft3d_c2c(x, size, order, order)) < TOL[prec]
 
 
+@pytest.mark.parametrize("order", [(0, 1, 2), (2, 0, 1), (1, 2, 0)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_executor_two_dimensions(gb, order, prec):
+    """The 2-D executor (the cufft_executor (d1, d2) constructor,
+    include/heffte_backend_cuda.h:459-481) on every pair of dimensions,
+    including (0, 2), the pair that needs the reference's embedded layout, and
+    the pair given in reverse order; forward and backward against the oracle
+    (two 1-D executor stages), in place and out of place."""
+    rng = np.random.default_rng(11)
+    size = (40, 24, 18)
+    n = int(np.prod(size))
+    box = gb.box3d((0, 0, 0), [s - 1 for s in size], order)
+    x = rand_c(rng, n, prec)
+    for dims in ([0, 1], [1, 2], [0, 2], [2, 0]):
+        ex = gb.executor(gb.kind.c2c, box, dims)
+        want = O.executor_c2c(O.executor_c2c(x, size, order, dims[0]), size, order, dims[1])
+        t = dev(x)
+        ex.forward(prec, t, t)
+        assert O.rel_l2(host(t), want) < TOL[prec], (dims, "forward")
+        o = torch.empty_like(t)
+        ex.backward(prec, t, o)
+        back = O.executor_c2c(O.executor_c2c(want, size, order, dims[0], 1), size, order, dims[1], 1)
+        assert O.rel_l2(host(o), back) < TOL[prec], (dims, "backward")
+        assert O.rel_l2(host(o), x * size[dims[0]] * size[dims[1]]) < 3 * TOL[prec], (dims, "round trip")
+    # a 2-D real-to-real executor (DCT-II along dimensions 0 and 2)
+    xr = rng.standard_normal(n).astype(rdt(prec))
+    ex = gb.executor(gb.kind.cos, box, [0, 2])
+    t = dev(xr)
+    ex.forward(prec, t, t)
+    c = O.to_canonical(xr, size, order)
+    for d in (0, 2):
+        c = np.moveaxis(O._r2r_forward_1d(O.COS, np.moveaxis(c, O.axis_of(d), -1)), -1, O.axis_of(d))
+    assert O.rel_l2(host(t), O.from_canonical(c, order)) < TOL[prec]
+
+
 # ---------------------------------------------------------------------------
 # fft3d / fft3d_r2c / rtransform against the reference fixtures and the oracle
 # ---------------------------------------------------------------------------

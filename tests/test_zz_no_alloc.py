@@ -86,7 +86,7 @@ def test_noalloc_rejects_inconsistent_strides(gb):
         (8, 4, 2, 8, 32, 8, -32),           # negative source plane stride
         (8, 4, 2, 8, 32, 3, 32),            # source lines overlap
         (8, 4, 2, 4, 32, 8, 32),            # destination lines overlap
-        (8, 4, 2, 8, 32, 8, 1 << 62),       # span overflows 63 bits
+        (8, 4, 3, 8, 32, 8, 1 << 62),       # span (2 x 2^62 + ...) overflows 63 bits
     ]
     for nf, nm, ns, ls, ps, bls, bps in bad:
         rc = L.heffte_gb300_transpose_unpack_inplace_noalloc(None, 0, nf, nm, ns, ls, ps, bls, bps, 0, 1, 2,
