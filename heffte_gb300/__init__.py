@@ -378,11 +378,15 @@ class executor:
     def workspace_size(self):
         return lib().heffte_gb300_executor_workspace_size(self._h)
 
-    def forward(self, prec, inp, out, stream=None):
-        check(lib().heffte_gb300_executor_forward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out), None))
+    def forward(self, prec, inp, out, stream=None, workspace=None):
+        """workspace: workspace_size() elements of the data type, or None
+        (the executor then keeps a buffer of its own)."""
+        check(lib().heffte_gb300_executor_forward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out),
+                                                  _ptr(workspace) if workspace is not None else None))
 
-    def backward(self, prec, inp, out, stream=None):
-        check(lib().heffte_gb300_executor_backward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out), None))
+    def backward(self, prec, inp, out, stream=None, workspace=None):
+        check(lib().heffte_gb300_executor_backward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out),
+                                                   _ptr(workspace) if workspace is not None else None))
 
 
 # -- location layer ---------------------------------------------------------

@@ -208,8 +208,9 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     long long in_off = 0, out_off = 0;
     for (auto const &s : sizes){
         for (int d = 0; d < 3; d++){
-            if (s[d] < 1 || !supported_length(s[d], prec))
-                throw Error(ST_UNSUPPORTED, "box side " + std::to_string(s[d]) + " is not supported");
+            if (s[d] < 1 || !direct_length(s[d]))
+                throw Error(ST_UNSUPPORTED, "box side " + std::to_string(s[d]) + " is not supported in a batch "
+                            "(sides up to " + std::to_string(kMaxDirectLength) + " with prime factors 2, 3, 5, 7, 11, 13)");
         }
         long long n = (long long)s[0] * s[1] * s[2];
         long long nc = r2c ? (long long)(s[0] / 2 + 1) * s[1] * s[2] : n;

@@ -187,23 +187,21 @@ long long heffte_gb300_executor_workspace_size(heffte_gb300_executor e){ return 
 
 int heffte_gb300_executor_forward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
                                   void *workspace){
-    (void)workspace;
     return guard([&]{
         if (!e) throw Error(ST_INVALID, "null executor");
         check_prec(prec);
         if (!in || !out) throw Error(ST_INVALID, "null pointer");
-        e->e->forward(as_stream(stream), prec, in, out);
+        e->e->forward(as_stream(stream), prec, in, out, workspace);
     });
 }
 
 int heffte_gb300_executor_backward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
                                    void *workspace){
-    (void)workspace;
     return guard([&]{
         if (!e) throw Error(ST_INVALID, "null executor");
         check_prec(prec);
         if (!in || !out) throw Error(ST_INVALID, "null pointer");
-        e->e->backward(as_stream(stream), prec, in, out);
+        e->e->backward(as_stream(stream), prec, in, out, workspace);
     });
 }
 

@@ -88,10 +88,7 @@ void const *Fft1D::r2r_twiddles(int prec, cudaStream_t s){
 // ---------------------------------------------------------------------------
 static const int kRadices[] = {16, 13, 11, 8, 7, 5, 4, 3, 2};
 
-int max_length(int prec){
-    // one transform must fit in shared memory and T = N / kEmax threads <= 512
-    return (prec == 0) ? 8192 : 8192;
-}
+int max_length(int){ return kMaxLength; }
 
 std::vector<int> default_radices(int N){
     // powers of two share the radix plan (and twiddle table) of the pipelined kernels
@@ -150,22 +147,65 @@ static Plan1D build_plan(int N, std::vector<int> const &radices, long long &tw_c
 }
 
 bool supported_length(int N, int prec){
-    if (N < 1 || N > max_length(prec)) return false;
+    return N >= 1 && N <= max_length(prec);
+}
+
+bool direct_length(int N){
     if (N == 1) return true;
-    return !default_radices(N).empty();
+    return N >= 1 && N <= kMaxDirectLength && !default_radices(N).empty();
+}
+
+// Split of a composite length with prime factors <= 13 into two direct
+// lengths: powers of two first (their pipelined kernels), then the most
+// balanced pair.  False when there is none.
+static bool fourstep_split(int N, int &N1, int &N2){
+    int best = -1;
+    double best_score = -1e30;
+    for (int d = std::max(2, (N + kMaxDirectLength - 1) / kMaxDirectLength); d <= kMaxDirectLength; d++){
+        if (N % d) continue;
+        int e = N / d;
+        if (e > kMaxDirectLength || !direct_length(d) || !direct_length(e)) continue;
+        auto pow2 = [](int v){ return (v & (v - 1)) == 0 ? 1 : 0; };
+        double score = 100.0 * (pow2(d) + pow2(e)) - std::fabs(std::log2((double)d) - std::log2((double)e));
+        if (score > best_score){ best_score = score; best = d; }
+    }
+    if (best < 0) return false;
+    N1 = best;
+    N2 = N / best;
+    return true;
 }
 
 std::shared_ptr<Fft1D> get_fft1d(int N, std::vector<int> const &radices){
-    static std::mutex mu;
+    // recursive: a composite length registers its factors (or Bluestein's length)
+    static std::recursive_mutex mu;
     static std::map<std::pair<int, std::vector<int>>, std::shared_ptr<Fft1D>> reg;
-    std::lock_guard<std::mutex> lk(mu);
+    std::lock_guard<std::recursive_mutex> lk(mu);
     auto key = std::make_pair(N, radices);
     auto it = reg.find(key);
     if (it != reg.end()) return it->second;
+    if (N < 1 || N > kMaxLength)
+        throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(N) + " is outside [1, " +
+                    std::to_string(kMaxLength) + "]");
+    if (radices.empty() && !direct_length(N)){
+        auto f = std::make_shared<Fft1D>();
+        f->N = N;
+        int N1 = 0, N2 = 0;
+        if (fourstep_split(N, N1, N2)){
+            f->algo = ALGO_FOURSTEP;
+            f->sub1 = get_fft1d(N1);
+            f->sub2 = get_fft1d(N2);
+        } else {
+            int M = 1;
+            while (M < 2 * N - 1) M *= 2;
+            f->algo = ALGO_BLUESTEIN;
+            f->sub1 = get_fft1d(M);
+        }
+        reg[key] = f;
+        return f;
+    }
     std::vector<int> rad = radices.empty() ? default_radices(N) : radices;
     if (N != 1 && rad.empty())
-        throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(N) +
-                    " has a prime factor above 13, which this backend does not support");
+        throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(N) + " has no radix plan");
     long long prod = 1;
     for (int r : rad){
         bool ok = false;
@@ -422,6 +462,10 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
 void launch_c2c(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (f.algo != ALGO_DIRECT){
+        launch_composite(s, LM_C2C, f, prec, fwd, 0, f.N, Li, Lo, in, out, G, scale, cfg);
+        return;
+    }
     if (cfg.tc && prec == 0 && tc_supported(f.N)){
         launch_tc_c2c(s, f.N, fwd, Li, Lo, in, out, G, scale);
         return;
@@ -457,6 +501,10 @@ bool launch_conv_pass(cudaStream_t s, Fft1D &f, int prec, Layout L, void *x, voi
 void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (f.algo != ALGO_DIRECT){
+        launch_composite(s, LM_R2C, f, prec, true, 0, f.N, Li, Lo, in, out, G, scale, cfg);
+        return;
+    }
     if (try_pipe(s, K_R2C, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
@@ -470,6 +518,10 @@ void launch_r2c(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void c
 void launch_c2r(cudaStream_t s, Fft1D &f, int prec, Layout Li, Layout Lo, void const *in, void *out,
                 long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (f.algo != ALGO_DIRECT){
+        launch_composite(s, LM_C2R, f, prec, false, 0, f.N, Li, Lo, in, out, G, scale, cfg);
+        return;
+    }
     if (try_pipe(s, K_C2R, f, prec, Li, Lo, in, out, G, scale, 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
@@ -484,6 +536,10 @@ void launch_dct1(cudaStream_t s, Fft1D &f, int prec, bool fwd, int N, Layout Li,
                  long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
     if (N < 2 || f.N != 2 * (N - 1)) throw Error(ST_INVALID, "DCT-I of N values runs on an FFT of length 2(N-1)");
+    if (f.algo != ALGO_DIRECT){
+        launch_composite(s, LM_DCT1, f, prec, true, 0, N, Li, Lo, in, out, G, fwd ? scale : 2.0 * scale, cfg);
+        return;
+    }
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);
     geometry(f, prec, cols, true, G, cfg, a);
@@ -498,6 +554,10 @@ void launch_dct1(cudaStream_t s, Fft1D &f, int prec, bool fwd, int N, Layout Li,
 void launch_r2r(cudaStream_t s, Fft1D &f, int prec, bool fwd, bool sine, Layout Li, Layout Lo, void const *in,
                 void *out, long long G, double scale, LaunchCfg cfg){
     if (G <= 0) return;
+    if (f.algo != ALGO_DIRECT){
+        launch_composite(s, fwd ? LM_R2R_F : LM_R2R_B, f, prec, fwd, sine ? 1 : 0, f.N, Li, Lo, in, out, G, scale, cfg);
+        return;
+    }
     if (try_pipe(s, fwd ? K_R2R_F : K_R2R_B, f, prec, Li, Lo, in, out, G, scale, sine ? 1 : 0, cfg)) return;
     KernelArgs a{};
     bool cols = is_cols(Li, Lo);

@@ -35,19 +35,38 @@ void set_last_error(std::string const &msg);
 // 1-D transform length: radix plan, thread count and device twiddle tables.
 // ---------------------------------------------------------------------------
 constexpr int kEmax = 16;
+// Lengths the radix kernels take directly: up to kMaxDirectLength with prime
+// factors 2, 3, 5, 7, 11, 13.  Longer lengths and other primes are composite
+// (gbfft_long.cu), up to kMaxLength.
+constexpr int kMaxDirectLength = 8192;
+constexpr int kMaxLength = 1 << 25;
+// Scratch bound of one chunk of lines of a composite length (complex elements).
+constexpr long long kCompositeScratchElems = 1LL << 26;
+
+// How a length is transformed: by the radix kernels, as N1 x N2 (four-step),
+// or by Bluestein's algorithm through a power-of-two length M >= 2N - 1.
+enum Algo { ALGO_DIRECT = 0, ALGO_FOURSTEP = 1, ALGO_BLUESTEIN = 2 };
+// Device tables of a composite length (per precision).
+enum CompositeTable { TAB_ROOTS = 0, TAB_CHIRP = 1, TAB_CHIRP_SPECTRUM = 2 };
 
 struct Fft1D {
     int N = 0;
     Plan1D plan{};
     std::vector<int> radices;
+    int algo = ALGO_DIRECT;
+    std::shared_ptr<Fft1D> sub1, sub2;    // four-step: N1, N2; Bluestein: M (sub1)
     // device tables, created lazily per precision: [0] float, [1] double
     void *tw[2] = {nullptr, nullptr};     // Stockham twiddles
     void *rtw[2] = {nullptr, nullptr};    // exp(-i pi k / 2N), k < N (r2r)
+    void *ctab[3][2] = {};                // composite tables (CompositeTable)
     long long tw_count = 0;
     std::mutex mu;
     ~Fft1D();
     void const *twiddles(int prec, cudaStream_t s);
     void const *r2r_twiddles(int prec, cudaStream_t s);
+    // four-step roots exp(-2 pi i m / N); Bluestein chirp exp(-i pi n^2 / N)
+    // and the spectrum of its conjugate on M points divided by M (FP64-generated)
+    void const *composite_table(int which, int prec, cudaStream_t s);
 };
 
 // Shared registry of lengths (plans are immutable once built; tables lazily).
@@ -55,6 +74,8 @@ struct Fft1D {
 std::shared_ptr<Fft1D> get_fft1d(int N, std::vector<int> const &radices = {});
 std::vector<int> default_radices(int N);
 bool supported_length(int N, int prec);
+// a length the radix kernels take directly (the batch and tensor-core kernels need one)
+bool direct_length(int N);
 int max_length(int prec);
 
 // Tuning knobs of one launch (chosen by the planner / autotuner).
@@ -63,7 +84,24 @@ struct LaunchCfg {
     int variant = 0;  // 0 = process-wide choice, 1 = generic kernels, 2 = pipelined kernels
     int tpb_div = 1;  // divides the automatic tile of the generic kernels
     int tc = 0;       // 1: complex<float> radix-16 stages on the tensor cores (split BF16)
+    void *scratch = nullptr;    // workspace of composite lengths (composite_scratch_elems)
+    size_t scratch_bytes = 0;
 };
+
+// Kinds of the gather / scatter around a composite transform (gbfft_long.cu).
+enum LineMode { LM_C2C = 0, LM_R2C = 1, LM_C2R = 2, LM_R2R_F = 3, LM_R2R_B = 4, LM_DCT1 = 5 };
+// Complex elements of scratch a batch of G lines of a composite length needs
+// (0 for direct lengths): two copies of a chunk of lines plus what
+// Bluestein's inner length needs; for the paired modes a unit is two lines.
+long long composite_scratch_elems(Fft1D const &f, int mode, long long G);
+long long composite_extra_per_line(Fft1D const &f);
+// Composite transform of `lines` contiguous lines X -> Y (X is kept; extra:
+// composite_extra_per_line(f) * lines complex elements).
+void composite_core(cudaStream_t s, Fft1D &f, int prec, bool fwd, void *X, void *Y, long long lines, void *extra);
+// The batched transform of a composite length in the caller's layouts (N is
+// the data length: the real length for r2c / c2r / r2r, the DCT-I length).
+void launch_composite(cudaStream_t s, int mode, Fft1D &f, int prec, bool fwd, int sine, int N, Layout Li, Layout Lo,
+                      void const *in, void *out, long long G, double scale, LaunchCfg const &cfg);
 
 // Tensor-core (tcgen05, split-BF16) complex<float> transforms of lengths
 // 16^s * {1, 2, 4, 8} in [64, 4096].

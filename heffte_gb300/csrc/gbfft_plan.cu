@@ -38,6 +38,21 @@ Layout pass_layout(Box3 const &box, int dim, std::array<int, 3> const &ref_order
 
 static long long batch_count(Box3 const &box, int dim){ return box.count() / box.size[dim]; }
 
+// offsets of buffers inside a workspace are rounded to 32 elements (256
+// bytes for complex<float>) so that they keep the workspace's alignment
+static long long round32(long long n){ return (n + 31) / 32 * 32; }
+
+// gather / scatter mode of a composite length for a kernel kind
+static int line_mode(int kernel_kind, bool dct1){
+    switch (kernel_kind){
+        case K_R2C: return LM_R2C;
+        case K_C2R: return LM_C2R;
+        case K_R2R_F: return dct1 ? LM_DCT1 : LM_R2R_F;
+        case K_R2R_B: return dct1 ? LM_DCT1 : LM_R2R_B;
+        default: return LM_C2C;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // executors
 // ---------------------------------------------------------------------------
@@ -56,49 +71,81 @@ std::unique_ptr<Executor> make_executor(int kind, Box3 const &box, std::vector<i
         if (kind == EX_COS1){
             // DCT-I of n values runs on an FFT of length 2(n - 1)
             if (n < 2 || !supported_length(2 * (n - 1), 1))
-                throw Error(ST_UNSUPPORTED, "DCT-I length " + std::to_string(n) + " is not supported (needs n >= 2 and 2(n-1) supported)");
+                throw Error(ST_UNSUPPORTED, "DCT-I length " + std::to_string(n) + " is not supported (needs n >= 2 and "
+                            "2(n-1) <= " + std::to_string(max_length(1)) + ")");
             e->ffts.push_back(get_fft1d(2 * (n - 1)));
-            continue;
+        } else {
+            if (!supported_length(n, 1))
+                throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(box.size[d]) + " is outside [1, " +
+                            std::to_string(max_length(1)) + "]");
+            e->ffts.push_back(get_fft1d(n));
         }
-        if (!supported_length(n, 1))
-            throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(box.size[d]) + " is not supported");
-        e->ffts.push_back(get_fft1d(n));
+        int mode = (kind == EX_C2C) ? LM_C2C : (kind == EX_R2C ? LM_R2C : (kind == EX_COS1 ? LM_DCT1 : LM_R2R_F));
+        e->scratch_elems = std::max(e->scratch_elems, composite_scratch_elems(*e->ffts.back(), mode, batch_count(box, d)));
     }
     return e;
 }
 
-void Executor::forward(cudaStream_t s, int prec, void const *in, void *out, double scale) const{
+Executor::~Executor(){
+    if (cached) cudaFree(cached);
+}
+
+LaunchCfg Executor::config(int prec, void *work) const{
+    LaunchCfg cfg;
+    size_t need = (size_t)scratch_elems * ((prec == 0) ? sizeof(float2) : sizeof(double2));
+    if (need == 0) return cfg;
+    if (!work){
+        std::lock_guard<std::mutex> lk(cache_mu);
+        if (cached_bytes < need){
+            if (cached) check_cuda(cudaFree(cached), "cudaFree(executor workspace)");
+            cached = nullptr;
+            cached_bytes = 0;
+            check_cuda(cudaMalloc(&cached, need), "cudaMalloc(executor workspace)");
+            cached_bytes = need;
+        }
+        work = cached;
+    }
+    cfg.scratch = work;
+    cfg.scratch_bytes = need;
+    return cfg;
+}
+
+void Executor::forward(cudaStream_t s, int prec, void const *in, void *out, void *work, double scale) const{
+    LaunchCfg cfg = config(prec, work);
     if (kind == EX_R2C){
         Box3 cb = box.r2c(dims[0]);
         launch_r2c(s, *ffts[0], prec, pass_layout(box, dims[0], box.order), pass_layout(cb, dims[0], box.order),
-                   in, out, batch_count(box, dims[0]), scale);
+                   in, out, batch_count(box, dims[0]), scale, cfg);
         return;
     }
     void const *src = in;
     for (size_t i = 0; i < dims.size(); i++){
         double sc = (i + 1 == dims.size()) ? scale : 1.0;
         Layout L = pass_layout(box, dims[i], box.order);
-        if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, true, L, L, src, out, batch_count(box, dims[i]), sc);
-        else if (kind == EX_COS1) launch_dct1(s, *ffts[i], prec, true, (int)box.size[dims[i]], L, L, src, out, batch_count(box, dims[i]), sc);
-        else launch_r2r(s, *ffts[i], prec, true, kind == EX_SIN, L, L, src, out, batch_count(box, dims[i]), sc);
+        long long G = batch_count(box, dims[i]);
+        if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, true, L, L, src, out, G, sc, cfg);
+        else if (kind == EX_COS1) launch_dct1(s, *ffts[i], prec, true, (int)box.size[dims[i]], L, L, src, out, G, sc, cfg);
+        else launch_r2r(s, *ffts[i], prec, true, kind == EX_SIN, L, L, src, out, G, sc, cfg);
         src = out;
     }
 }
 
-void Executor::backward(cudaStream_t s, int prec, void const *in, void *out, double scale) const{
+void Executor::backward(cudaStream_t s, int prec, void const *in, void *out, void *work, double scale) const{
+    LaunchCfg cfg = config(prec, work);
     if (kind == EX_R2C){
         Box3 cb = box.r2c(dims[0]);
         launch_c2r(s, *ffts[0], prec, pass_layout(cb, dims[0], box.order), pass_layout(box, dims[0], box.order),
-                   in, out, batch_count(box, dims[0]), scale);
+                   in, out, batch_count(box, dims[0]), scale, cfg);
         return;
     }
     void const *src = in;
     for (size_t i = 0; i < dims.size(); i++){
         double sc = (i + 1 == dims.size()) ? scale : 1.0;
         Layout L = pass_layout(box, dims[i], box.order);
-        if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, false, L, L, src, out, batch_count(box, dims[i]), sc);
-        else if (kind == EX_COS1) launch_dct1(s, *ffts[i], prec, false, (int)box.size[dims[i]], L, L, src, out, batch_count(box, dims[i]), sc);
-        else launch_r2r(s, *ffts[i], prec, false, kind == EX_SIN, L, L, src, out, batch_count(box, dims[i]), sc);
+        long long G = batch_count(box, dims[i]);
+        if (kind == EX_C2C) launch_c2c(s, *ffts[i], prec, false, L, L, src, out, G, sc, cfg);
+        else if (kind == EX_COS1) launch_dct1(s, *ffts[i], prec, false, (int)box.size[dims[i]], L, L, src, out, G, sc, cfg);
+        else launch_r2r(s, *ffts[i], prec, false, kind == EX_SIN, L, L, src, out, G, sc, cfg);
         src = out;
     }
 }
@@ -276,13 +323,12 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         if (kind == PK_COS1){
             if (n < 2 || !supported_length(2 * (n - 1), 1))
                 throw Error(ST_UNSUPPORTED, "DCT-I length " + std::to_string(n) + " is not supported (needs n >= 2 and "
-                            "2(n-1) with prime factors 2, 3, 5, 7, 11, 13 up to " + std::to_string(max_length(1)) + ")");
+                            "2(n-1) <= " + std::to_string(max_length(1)) + ")");
             continue;
         }
         if (!supported_length(n, 1))
-            throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(n) +
-                        " is not supported (lengths up to " + std::to_string(max_length(1)) +
-                        " with prime factors 2, 3, 5, 7, 11, 13)");
+            throw Error(ST_UNSUPPORTED, "transform length " + std::to_string(n) + " is outside [1, " +
+                        std::to_string(max_length(1)) + "]");
     }
     std::array<int, 3> io = inbox.order, oo = outbox.order;
     bool reorder = o.use_reorder;
@@ -331,6 +377,21 @@ std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbo
         p->work_buf_elems = per;
         p->work_elems = std::max(std::max(wf, wfa), wb) * per;
         p->scale_factor = 1.0 / (double)inbox.count();
+    }
+    // composite lengths (four-step, Bluestein) run in a scratch region after
+    // the work buffers, sized for the largest batch of lines of any pass
+    long long sc = 0;
+    for (auto const *ops : {&p->fwd, &p->fwd_alias, &p->bwd})
+        for (auto const &op : *ops)
+            if (op.type == Op::FFT)
+                sc = std::max(sc, composite_scratch_elems(*op.fft, line_mode(op.kind, kind == PK_COS1),
+                                                          op.sbox.count() / op.sbox.size[op.dim]));
+    if (sc > 0){
+        // workspace elements are complex for c2c / r2c plans, real for r2r plans
+        long long per_complex = (kind == PK_C2C || kind == PK_R2C) ? 1 : 2;
+        p->scratch_elems = sc;
+        p->scratch_offset = round32(p->work_elems);
+        p->work_elems = p->scratch_offset + per_complex * sc;
     }
     return p;
 }
@@ -386,6 +447,10 @@ void Plan3D::execute(bool forward, int prec, int batch, void const *in, void *ou
     cfg.variant = (knobs.variant == 1) ? 1 : 0;
     cfg.tpb_div = std::max(1, knobs.tile_div);
     cfg.tc = knobs.tensor_cores;
+    if (scratch_elems > 0){
+        cfg.scratch = wbase + (size_t)scratch_offset * work_es;
+        cfg.scratch_bytes = (size_t)scratch_elems * ((prec == 0) ? sizeof(float2) : sizeof(double2));
+    }
     for (int j = 0; j < batch; j++){
         void *bufs[4];
         bufs[0] = const_cast<char*>(reinterpret_cast<char const*>(in)) + (size_t)j * in_cnt * in_es;
@@ -456,9 +521,6 @@ Box3 Plan3D::conv_box() const{
     return b;
 }
 
-// offsets of the spectrum boxes in the workspace, rounded to 32 elements
-// (256 bytes) so that they keep the alignment of the workspace itself
-static long long round32(long long n){ return (n + 31) / 32 * 32; }
 
 long long Plan3D::convolve_workspace() const{
     return round32(work_elems) + 2 * round32(std::max(conv_box().alloc_count(), size_outbox()));

@@ -58,11 +58,20 @@ struct Executor {
     Box3 box;
     std::vector<int> dims;
     std::vector<std::shared_ptr<Fft1D>> ffts;
+    long long scratch_elems = 0;          // complex elements the composite lengths need (0: none)
+    mutable void *cached = nullptr;       // used when the caller passes no workspace
+    mutable size_t cached_bytes = 0;
+    mutable std::mutex cache_mu;
+    ~Executor();
     long long box_size() const { return box.count(); }
     long long complex_size() const { return (kind == EX_R2C) ? box.r2c(dims[0]).count() : box.count(); }
-    long long workspace_size() const { return 0; }
-    void forward(cudaStream_t s, int prec, void const *in, void *out, double scale = 1.0) const;
-    void backward(cudaStream_t s, int prec, void const *in, void *out, double scale = 1.0) const;
+    // in elements of the executor's data type: complex for c2c / r2c, real for r2r
+    long long workspace_size() const { return (kind == EX_C2C || kind == EX_R2C) ? scratch_elems : 2 * scratch_elems; }
+    // work: workspace_size() elements, or null (the executor then keeps a buffer of its own)
+    void forward(cudaStream_t s, int prec, void const *in, void *out, void *work = nullptr, double scale = 1.0) const;
+    void backward(cudaStream_t s, int prec, void const *in, void *out, void *work = nullptr, double scale = 1.0) const;
+private:
+    LaunchCfg config(int prec, void *work) const;
 };
 std::unique_ptr<Executor> make_executor(int kind, Box3 const &box, std::vector<int> const &dims);
 
@@ -113,6 +122,8 @@ struct Plan3D {
     std::vector<Op> fwd, fwd_alias, bwd;
     long long work_elems = 0;     // workspace in output-type elements (complex for c2c/r2c)
     long long work_buf_elems = 0; // elements of one of the (up to two) workspace buffers
+    long long scratch_elems = 0;  // complex elements of scratch for composite lengths (four-step, Bluestein)
+    long long scratch_offset = 0; // where that scratch starts in the workspace (workspace elements)
     double scale_factor = 1.0;    // "full" factor
     void *cached_work = nullptr;  // lazily allocated when the caller passes no workspace
     size_t cached_bytes = 0;

@@ -139,7 +139,7 @@ int tune_lengths(std::vector<int> const &lengths, int prec, cudaStream_t s, std:
             std::lock_guard<std::mutex> lk(g_mu);
             if (g_table.count({prec, N})) continue;
         }
-        if (!supported_length(N, prec) || N < 2) continue;
+        if (!direct_length(N) || N < 2) continue;
         // boxes of N^3, enough of them for about 2^24 values per batch
         long long per = (long long)N * N * N;
         int nbox = (int)std::max<long long>(1, std::min<long long>(64, (1LL << 24) / per));

@@ -83,14 +83,16 @@ namespace gb300 {
         ~executor_handle(){ if (handle) heffte_gb300_executor_destroy(handle); }
         executor_handle(executor_handle const&) = delete;
         executor_handle& operator =(executor_handle const&) = delete;
-        void forward(cudaStream_t s, int prec, void const *in, void *out) const{
-            check(heffte_gb300_executor_forward(handle, s, prec, in, out, nullptr), "heffte_gb300_executor_forward()");
+        void forward(cudaStream_t s, int prec, void const *in, void *out, void *work) const{
+            check(heffte_gb300_executor_forward(handle, s, prec, in, out, work), "heffte_gb300_executor_forward()");
         }
-        void backward(cudaStream_t s, int prec, void const *in, void *out) const{
-            check(heffte_gb300_executor_backward(handle, s, prec, in, out, nullptr), "heffte_gb300_executor_backward()");
+        void backward(cudaStream_t s, int prec, void const *in, void *out, void *work) const{
+            check(heffte_gb300_executor_backward(handle, s, prec, in, out, work), "heffte_gb300_executor_backward()");
         }
         long long box_size() const{ return heffte_gb300_executor_box_size(handle); }
         long long complex_size() const{ return heffte_gb300_executor_complex_size(handle); }
+        //! \brief Elements of the executor's data type the composite lengths need (executor_base::workspace_size).
+        size_t workspace_size() const{ return static_cast<size_t>(heffte_gb300_executor_workspace_size(handle)); }
     private:
         heffte_gb300_executor handle = nullptr;
     };
@@ -115,10 +117,10 @@ public:
     gb300_executor(cudaStream_t s, box3d<index> const box)
         : stream(s), total(box.count()), exec(HEFFTE_GB300_C2C, box, {0, 1, 2}){}
 
-    void forward(std::complex<float> data[], std::complex<float>*) const override{ exec.forward(stream, 0, data, data); }
-    void backward(std::complex<float> data[], std::complex<float>*) const override{ exec.backward(stream, 0, data, data); }
-    void forward(std::complex<double> data[], std::complex<double>*) const override{ exec.forward(stream, 1, data, data); }
-    void backward(std::complex<double> data[], std::complex<double>*) const override{ exec.backward(stream, 1, data, data); }
+    void forward(std::complex<float> data[], std::complex<float> *w) const override{ exec.forward(stream, 0, data, data, w); }
+    void backward(std::complex<float> data[], std::complex<float> *w) const override{ exec.backward(stream, 0, data, data, w); }
+    void forward(std::complex<double> data[], std::complex<double> *w) const override{ exec.forward(stream, 1, data, data, w); }
+    void backward(std::complex<double> data[], std::complex<double> *w) const override{ exec.backward(stream, 1, data, data, w); }
     // real input through the complex transform, as cufft_executor (:527-545)
     void forward(float const indata[], std::complex<float> outdata[], std::complex<float> *w) const override{
         gb300::check(heffte_gb300_convert(stream, 0, total, indata, outdata, 1), "heffte_gb300_convert()");
@@ -137,7 +139,7 @@ public:
         gb300::check(heffte_gb300_convert(stream, 1, total, indata, outdata, 0), "heffte_gb300_convert()");
     }
     int box_size() const override{ return static_cast<int>(total); }
-    size_t workspace_size() const override{ return 0; }
+    size_t workspace_size() const override{ return exec.workspace_size(); }
 private:
     cudaStream_t stream;
     long long total;
@@ -155,21 +157,21 @@ public:
     template<typename index>
     gb300_executor_r2c(cudaStream_t s, box3d<index> const box, int dimension)
         : stream(s), exec(HEFFTE_GB300_R2C, box, {dimension}){}
-    void forward(float const indata[], std::complex<float> outdata[], std::complex<float>*) const override{
-        exec.forward(stream, 0, indata, outdata);
+    void forward(float const indata[], std::complex<float> outdata[], std::complex<float> *w) const override{
+        exec.forward(stream, 0, indata, outdata, w);
     }
-    void backward(std::complex<float> indata[], float outdata[], std::complex<float>*) const override{
-        exec.backward(stream, 0, indata, outdata);
+    void backward(std::complex<float> indata[], float outdata[], std::complex<float> *w) const override{
+        exec.backward(stream, 0, indata, outdata, w);
     }
-    void forward(double const indata[], std::complex<double> outdata[], std::complex<double>*) const override{
-        exec.forward(stream, 1, indata, outdata);
+    void forward(double const indata[], std::complex<double> outdata[], std::complex<double> *w) const override{
+        exec.forward(stream, 1, indata, outdata, w);
     }
-    void backward(std::complex<double> indata[], double outdata[], std::complex<double>*) const override{
-        exec.backward(stream, 1, indata, outdata);
+    void backward(std::complex<double> indata[], double outdata[], std::complex<double> *w) const override{
+        exec.backward(stream, 1, indata, outdata, w);
     }
     int box_size() const override{ return static_cast<int>(exec.box_size()); }
     int complex_size() const override{ return static_cast<int>(exec.complex_size()); }
-    size_t workspace_size() const override{ return 0; }
+    size_t workspace_size() const override{ return exec.workspace_size(); }
 private:
     cudaStream_t stream;
     gb300::executor_handle exec;
@@ -195,12 +197,12 @@ public:
     template<typename index>
     gb300_r2r_executor(cudaStream_t s, box3d<index> const box)
         : stream(s), exec(kind, box, {0, 1, 2}){}
-    void forward(float data[], float*) const override{ exec.forward(stream, 0, data, data); }
-    void forward(double data[], double*) const override{ exec.forward(stream, 1, data, data); }
-    void backward(float data[], float*) const override{ exec.backward(stream, 0, data, data); }
-    void backward(double data[], double*) const override{ exec.backward(stream, 1, data, data); }
+    void forward(float data[], float *w) const override{ exec.forward(stream, 0, data, data, w); }
+    void forward(double data[], double *w) const override{ exec.forward(stream, 1, data, data, w); }
+    void backward(float data[], float *w) const override{ exec.backward(stream, 0, data, data, w); }
+    void backward(double data[], double *w) const override{ exec.backward(stream, 1, data, data, w); }
     int box_size() const override{ return static_cast<int>(exec.box_size()); }
-    size_t workspace_size() const override{ return 0; }
+    size_t workspace_size() const override{ return exec.workspace_size(); }
 private:
     cudaStream_t stream;
     gb300::executor_handle exec;

@@ -30,7 +30,7 @@ extern "C" {
 #define HEFFTE_GB300_SUCCESS 0
 #define HEFFTE_GB300_INVALID 1      /* bad geometry, null pointer, bad option   */
 #define HEFFTE_GB300_CUDA_ERROR 2   /* a CUDA runtime call or launch failed     */
-#define HEFFTE_GB300_UNSUPPORTED 3  /* e.g. a transform length with a prime > 13 */
+#define HEFFTE_GB300_UNSUPPORTED 3  /* e.g. a transform length above 2^25           */
 #define HEFFTE_GB300_ALLOC_ERROR 4  /* device allocation failed                  */
 
 /* element types: float, double, std::complex<float>, std::complex<double> */
@@ -163,14 +163,21 @@ typedef struct heffte_gb300_executor_s *heffte_gb300_executor;
 int heffte_gb300_executor_create(int kind, const long long low[3], const long long high[3], const int order[3],
                                  int ndims, const int dims[3], heffte_gb300_executor *out);
 int heffte_gb300_executor_destroy(heffte_gb300_executor e);
-/* executor_base::box_size / complex_size / workspace_size (include/heffte_common.h:585-594) */
+/* executor_base::box_size / complex_size / workspace_size (include/heffte_common.h:585-594).
+ * The workspace is counted in elements of the executor's data type (complex
+ * for C2C / R2C, real for COS / SIN / COS1, of the precision of each call);
+ * it is 0 unless a length is transformed by the composite algorithms: lengths
+ * above 8192 (four-step, N = N1 N2) and lengths with a prime factor above 13
+ * (Bluestein's algorithm), which the cufft_executor role also accepts
+ * (include/heffte_backend_cuda.h:346-422). */
 long long heffte_gb300_executor_box_size(heffte_gb300_executor e);
 long long heffte_gb300_executor_complex_size(heffte_gb300_executor e);
 long long heffte_gb300_executor_workspace_size(heffte_gb300_executor e);
 /* Forward / backward.  C2C and COS/SIN: in-place when in == out (the
  * reference signature forward(data[], workspace)); R2C forward: real in ->
  * complex out; R2C backward: complex in -> real out (the input is not modified).
- * prec 0 = single, 1 = double.  workspace may be NULL (size 0). */
+ * prec 0 = single, 1 = double.  workspace: workspace_size() elements, or NULL
+ * (the executor then allocates one buffer of its own once and keeps it). */
 int heffte_gb300_executor_forward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,
                                   void *workspace);
 int heffte_gb300_executor_backward(heffte_gb300_executor e, void *stream, int prec, const void *in, void *out,

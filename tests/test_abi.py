@@ -61,19 +61,43 @@ def test_plan_rejects_bad_geometry(gb):
 
 
 def test_plan_rejects_unsupported_length(gb):
+    n = (1 << 25) + 1                           # above the longest transform, 2^25
     with pytest.raises(gb.HeffteError) as e:
-        gb.fft3d(gb.box3d((0, 0, 0), (16, 7, 7)), gb.box3d((0, 0, 0), (16, 7, 7)))  # 17 is prime > 13
-    assert e.value.code == 3 and "17" in str(e.value)
+        gb.fft3d(gb.box3d((0, 0, 0), (n - 1, 0, 0)), gb.box3d((0, 0, 0), (n - 1, 0, 0)))
+    assert e.value.code == 3 and str(n) in str(e.value)
+
+
+def test_composite_lengths_plan_with_a_workspace(gb):
+    """Lengths with a prime factor above 13 (Bluestein) and above 8192
+    (four-step) are planned like any other; their scratch is part of the
+    plan's workspace, and the executors report theirs (no GPU needed)."""
+    for size in ((17, 8, 6), (17, 23, 29), (16384, 2, 2), (8191, 1, 2)):
+        b = gb.box3d((0, 0, 0), [s - 1 for s in size])
+        p = gb.fft3d(b, b)
+        assert p.size_workspace() > 0, size
+        r = gb.fft3d_r2c(b, b.r2c(0), 0)
+        assert r.size_workspace() > 0, size
+    b = gb.box3d((0, 0, 0), (63, 31, 15))
+    assert gb.fft3d(b, b).size_workspace() == 0          # direct lengths, no reshapes: none
+    ex = gb.executor(gb.kind.c2c, gb.box3d((0, 0, 0), (96, 3, 2)), [0])
+    assert ex.workspace_size() >= 2 * 97 * 12            # two copies of the lines, plus Bluestein's
+    ex = gb.executor(gb.kind.cos, gb.box3d((0, 0, 0), (96, 3, 2)), [0])
+    assert ex.workspace_size() % 2 == 0 and ex.workspace_size() > 0   # real elements
+    with pytest.raises(gb.HeffteError) as e:
+        gb.boxbatch(gb.kind.r2c, [(17, 16, 16)])       # the batch kernel takes direct lengths only
+    assert e.value.code == 3
 
 
 def test_dct1_plans_and_scale(gb):
-    """rtransform<cos1>: lengths n >= 2 whose 2(n-1) factors into 2..13, scale
-    1/(64 prod(n_i - 1)) (include/heffte_fft3d.h:643-647)."""
+    """rtransform<cos1>: lengths n >= 2, scale 1/(64 prod(n_i - 1))
+    (include/heffte_fft3d.h:643-647)."""
     b = gb.box3d((0, 0, 0), (32, 24, 16))           # 33 x 25 x 17: FFTs of 64, 48, 32
     p = gb.rtransform(gb.kind.cos1, b, b)
     assert p.size_inbox() == 33 * 25 * 17
     assert p.get_scale_factor(gb.scale.full) == pytest.approx(1.0 / (64 * 32 * 24 * 16))
-    for bad in ((31, 7, 7), (0, 7, 7)):                # 2 * 31 = 62 has the factor 31; n = 1
+    b = gb.box3d((0, 0, 0), (31, 7, 7))              # 2 * 31 = 62: Bluestein's FFT
+    assert gb.rtransform(gb.kind.cos1, b, b).size_workspace() > 0
+    for bad in ((0, 7, 7), ((1 << 24) + 1, 7, 7)):    # n = 1; 2(n - 1) above 2^25
         with pytest.raises(gb.HeffteError) as e:
             bb = gb.box3d((0, 0, 0), bad)
             gb.rtransform(gb.kind.cos1, bb, bb)
