@@ -65,6 +65,16 @@ def lib():
         getattr(L, "heffte_gb300_executor_" + f).restype = ll
     L.heffte_gb300_executor_forward.argtypes = [vp, vp, i, vp, vp, vp]
     L.heffte_gb300_executor_backward.argtypes = [vp, vp, i, vp, vp, vp]
+    L.heffte_gb300_reshape_create.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(vp)]
+    L.heffte_gb300_reshape_destroy.argtypes = [vp]
+    for f in ("send_size", "recv_size"):
+        getattr(L, "heffte_gb300_reshape_" + f).argtypes = [vp]
+        getattr(L, "heffte_gb300_reshape_" + f).restype = ll
+    llp = ctypes.POINTER(ll)
+    L.heffte_gb300_reshape_counts.argtypes = [vp, llp, llp, llp, llp]
+    L.heffte_gb300_reshape_pack.argtypes = [vp, vp, i, vp, vp]
+    L.heffte_gb300_reshape_unpack.argtypes = [vp, vp, i, vp, vp]
     L.heffte_gb300_set_default_options.argtypes = [ctypes.c_void_p]
     L.heffte_gb300_plan_create.argtypes = [i, I3, I3, I3, I3, I3, I3, i, vp, vp, ctypes.POINTER(vp)]
     L.heffte_gb300_plan_destroy.argtypes = [vp]
@@ -387,6 +397,45 @@ class executor:
     def backward(self, prec, inp, out, stream=None, workspace=None):
         check(lib().heffte_gb300_executor_backward(self._h, _stream_handle(stream), prec, _ptr(inp), _ptr(out),
                                                    _ptr(workspace) if workspace is not None else None))
+
+
+class reshape3d:
+    """reshape3d_alltoallv (src/heffte_reshape3d.cpp:365-496) of rank `me`:
+    moves data from every rank's input box to every rank's output box.
+    inboxes / outboxes: the box3d of every rank of the group.  pack() fills a
+    send buffer, unpack() empties a receive buffer, both on the device; the
+    exchange between them (counts(): elements per rank, rank order) is the
+    caller's all-to-all."""
+
+    def __init__(self, inboxes, outboxes, me):
+        self.nranks = len(inboxes)
+        self.me = me
+        flat = lambda bs: (ctypes.c_int * (9 * len(bs)))(*[int(v) for b in bs for v in (*b.low, *b.high, *b.order)])
+        self._h = ctypes.c_void_p()
+        check(lib().heffte_gb300_reshape_create(self.nranks, me, flat(inboxes), flat(outboxes), ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.heffte_gb300_reshape_destroy(h)
+
+    def send_size(self):
+        return lib().heffte_gb300_reshape_send_size(self._h)
+
+    def recv_size(self):
+        return lib().heffte_gb300_reshape_recv_size(self._h)
+
+    def counts(self):
+        """(send_counts, send_displs, recv_counts, recv_displs), lists of nranks ints."""
+        arrs = [(ctypes.c_longlong * self.nranks)() for _ in range(4)]
+        check(lib().heffte_gb300_reshape_counts(self._h, *arrs))
+        return tuple(list(a) for a in arrs)
+
+    def pack(self, dtype, inp, send_buffer, stream=None):
+        check(lib().heffte_gb300_reshape_pack(self._h, _stream_handle(stream), dtype, _ptr(inp), _ptr(send_buffer)))
+
+    def unpack(self, dtype, recv_buffer, out, stream=None):
+        check(lib().heffte_gb300_reshape_unpack(self._h, _stream_handle(stream), dtype, _ptr(recv_buffer), _ptr(out)))
 
 
 # -- location layer ---------------------------------------------------------

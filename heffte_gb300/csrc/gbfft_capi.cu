@@ -206,6 +206,70 @@ int heffte_gb300_executor_backward(heffte_gb300_executor e, void *stream, int pr
 }
 
 // ---------------------------------------------------------------------------
+struct heffte_gb300_reshape_s { std::unique_ptr<Reshape> r; };
+
+int heffte_gb300_reshape_create(int nranks, int me, const int *inboxes, const int *outboxes,
+                                heffte_gb300_reshape *out){
+    return guard([&]{
+        if (!out || !inboxes || !outboxes) throw Error(ST_INVALID, "null pointer");
+        *out = nullptr;
+        if (nranks < 1) throw Error(ST_INVALID, "a reshape needs at least one rank");
+        std::vector<Box3> ib, ob;
+        for (int r = 0; r < nranks; r++){
+            int const *a = inboxes + 9 * r, *b = outboxes + 9 * r;
+            ib.emplace_back(std::array<long long, 3>{a[0], a[1], a[2]}, std::array<long long, 3>{a[3], a[4], a[5]},
+                            order_of(a + 6));
+            ob.emplace_back(std::array<long long, 3>{b[0], b[1], b[2]}, std::array<long long, 3>{b[3], b[4], b[5]},
+                            order_of(b + 6));
+        }
+        auto R = make_reshape(nranks, me, ib, ob);
+        auto *h = new heffte_gb300_reshape_s;
+        h->r = std::move(R);
+        *out = h;
+    });
+}
+
+int heffte_gb300_reshape_destroy(heffte_gb300_reshape r){ return guard([&]{ delete r; }); }
+long long heffte_gb300_reshape_send_size(heffte_gb300_reshape r){ return r ? r->r->send_total : -1; }
+long long heffte_gb300_reshape_recv_size(heffte_gb300_reshape r){ return r ? r->r->recv_total : -1; }
+
+int heffte_gb300_reshape_counts(heffte_gb300_reshape r, long long *send_counts, long long *send_displs,
+                                long long *recv_counts, long long *recv_displs){
+    return guard([&]{
+        if (!r) throw Error(ST_INVALID, "null reshape");
+        Reshape const &R = *r->r;
+        for (int i = 0; i < R.nranks; i++){
+            if (send_counts) send_counts[i] = R.send_counts[i];
+            if (send_displs) send_displs[i] = R.send_displs[i];
+            if (recv_counts) recv_counts[i] = R.recv_counts[i];
+            if (recv_displs) recv_displs[i] = R.recv_displs[i];
+        }
+    });
+}
+
+int heffte_gb300_reshape_pack(heffte_gb300_reshape r, void *stream, int dtype, const void *input, void *send_buffer){
+    return guard([&]{
+        if (!r) throw Error(ST_INVALID, "null reshape");
+        check_dtype(dtype);
+        if (r->r->send_total == 0) return;
+        if (!input || !send_buffer) throw Error(ST_INVALID, "null pointer");
+        r->r->pack(as_stream(stream), dtype, input, send_buffer);
+        check_cuda(cudaPeekAtLastError(), "reshape pack");
+    });
+}
+
+int heffte_gb300_reshape_unpack(heffte_gb300_reshape r, void *stream, int dtype, const void *recv_buffer, void *output){
+    return guard([&]{
+        if (!r) throw Error(ST_INVALID, "null reshape");
+        check_dtype(dtype);
+        if (r->r->recv_total == 0) return;
+        if (!recv_buffer || !output) throw Error(ST_INVALID, "null pointer");
+        r->r->unpack(as_stream(stream), dtype, recv_buffer, output);
+        check_cuda(cudaPeekAtLastError(), "reshape unpack");
+    });
+}
+
+// ---------------------------------------------------------------------------
 int heffte_gb300_set_default_options(heffte_gb300_plan_options *o){
     return guard([&]{
         if (!o) throw Error(ST_INVALID, "null options");

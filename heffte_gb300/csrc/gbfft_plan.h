@@ -153,6 +153,30 @@ struct Plan3D {
     int convolve_fused_dim(int prec, void *xb, void const *yb) const;
 };
 
+// reshape3d_alltoallv of one rank of a group (src/heffte_reshape3d.cpp:365-496):
+// the overlaps this rank sends and receives, packed / unpacked on the device;
+// the exchange between the buffers is the caller's (gbfft_reshape.cu).
+struct Reshape {
+    struct Chunk {
+        int rank = 0;                      // the other rank
+        long long box_offset = 0;          // first element of the overlap in this rank's box
+        std::array<long long, 3> size{};   // fast, mid, slow extents of the overlap (this rank's order)
+        long long line_stride = 0, plane_stride = 0;      // of this rank's box
+        std::array<int, 3> map{0, 1, 2};   // received chunks: the sender's fast / mid / slow -> this rank's
+        long long buff_line_stride = 0, buff_plane_stride = 0;   // of the received chunk
+    };
+    int nranks = 1, me = 0;
+    Box3 inbox, outbox;
+    std::vector<Chunk> send, recv;
+    // elements per rank (rank order) of the send / receive buffers
+    std::vector<long long> send_counts, send_displs, recv_counts, recv_displs;
+    long long send_total = 0, recv_total = 0;
+    void pack(cudaStream_t s, int dtype, void const *input, void *send_buffer) const;
+    void unpack(cudaStream_t s, int dtype, void const *recv_buffer, void *output) const;
+};
+std::unique_ptr<Reshape> make_reshape(int nranks, int me, std::vector<Box3> const &inboxes,
+                                      std::vector<Box3> const &outboxes);
+
 std::unique_ptr<Plan3D> make_plan(int kind, Box3 const &inbox, Box3 const &outbox, int r2c_dir, Options const &o,
                                   cudaStream_t stream, Knobs const &knobs = Knobs{});
 

@@ -225,6 +225,21 @@ template<> struct one_dim_backend<backend::gb300_cos1>{
     using executor_r2c = void;
 };
 
+// No 3-D executor for the gb300 tags: fft3d::setup puts a 3-D executor in the
+// first of its three executor slots (include/heffte_fft3d.h:607-608), so the
+// backward executor list begins with a null slot, and compute_transform's
+// branch for a single active reshape copies the input into its temporary
+// buffer only when that first slot is set (src/heffte_compute_transform.cpp:
+// 73-80).  Backward transforms with use_reorder = false and different input
+// and output orders (the last reshape alone active) then transform an
+// uninitialised buffer; the cuFFT tags, for which has_executor3d is also
+// true, take the same branch.  The 2-D + 1-D executors fft3d::setup picks
+// instead run the same passes and keep the first backward slot set.
+template<> constexpr bool has_executor3d<backend::gb300>(){ return false; }
+template<> constexpr bool has_executor3d<backend::gb300_cos>(){ return false; }
+template<> constexpr bool has_executor3d<backend::gb300_sin>(){ return false; }
+template<> constexpr bool has_executor3d<backend::gb300_cos1>(){ return false; }
+
 // strided executors are the fast path: no transposes by default
 template<> struct default_plan_options<backend::gb300>{ static const bool use_reorder = false; };
 template<> struct default_plan_options<backend::gb300_cos>{ static const bool use_reorder = false; };

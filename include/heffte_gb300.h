@@ -184,6 +184,38 @@ int heffte_gb300_executor_backward(heffte_gb300_executor e, void *stream, int pr
                                    void *workspace);
 
 /* ======================================================================= */
+/* 2b. Reshapes between the box decompositions of a group of ranks          */
+/* ======================================================================= */
+
+/* Replaces reshape3d_alltoallv (src/heffte_reshape3d.cpp:365-443, built by
+ * make_reshape3d_alltoallv, :445-496) on rank `me` of `nranks`, one GPU per
+ * rank.  inboxes / outboxes hold 9 ints per rank (low[3], high[3], order[3])
+ * for every rank of the group, as mpi::gather_boxes gives them
+ * (include/heffte_geometry.h:707-718).  This rank sends the overlap of its
+ * input box with each rank's output box and receives the overlap of its
+ * output box with each rank's input box.  pack() gathers the outgoing
+ * overlaps into one send buffer (send_size() elements, rank r's part at
+ * send_displs[r], send_counts[r] elements, in this rank's input order);
+ * unpack() scatters a receive buffer laid out the same way (recv_counts,
+ * recv_displs) into the output box, transposing chunks whose sender's order
+ * differs.  The exchange between the two, the reference's MPI_Alltoallv, is
+ * the caller's (MPI_Alltoallv, NCCL send / recv, or a host-staged all-to-all).
+ * Bit-exact copies; dtype as for direct_pack. */
+typedef struct heffte_gb300_reshape_s *heffte_gb300_reshape;
+int heffte_gb300_reshape_create(int nranks, int me, const int *inboxes, const int *outboxes,
+                                heffte_gb300_reshape *reshape);
+int heffte_gb300_reshape_destroy(heffte_gb300_reshape reshape);
+long long heffte_gb300_reshape_send_size(heffte_gb300_reshape reshape);
+long long heffte_gb300_reshape_recv_size(heffte_gb300_reshape reshape);
+/* nranks entries each (any pointer may be NULL) */
+int heffte_gb300_reshape_counts(heffte_gb300_reshape reshape, long long *send_counts, long long *send_displs,
+                                long long *recv_counts, long long *recv_displs);
+int heffte_gb300_reshape_pack(heffte_gb300_reshape reshape, void *stream, int dtype, const void *input,
+                              void *send_buffer);
+int heffte_gb300_reshape_unpack(heffte_gb300_reshape reshape, void *stream, int dtype, const void *recv_buffer,
+                                void *output);
+
+/* ======================================================================= */
 /* 3. 3-D plans: fft3d / fft3d_r2c / rtransform on one rank                 */
 /* ======================================================================= */
 

@@ -309,6 +309,99 @@ def transpose_unpack(buf, dst, size, line_stride, plane_stride, buff_line_stride
     return out
 
 
+# --------------------------------------------------------------------------
+# multi-rank reshape (reshape3d_alltoallv, src/heffte_reshape3d.cpp:147-233,
+# 365-496): boxes are (low, high, order) triples
+# --------------------------------------------------------------------------
+def _osize(box, d):
+    lo, hi, order = box
+    return hi[order[d]] - lo[order[d]] + 1
+
+
+def box_count(box):
+    lo, hi, _ = box
+    return max(0, int(np.prod([hi[d] - lo[d] + 1 for d in range(3)]))) if all(hi[d] >= lo[d] for d in range(3)) else 0
+
+
+def collide(a, b):
+    """box3d::collide: the intersection in the order of `a` (None if empty)."""
+    lo = tuple(max(a[0][d], b[0][d]) for d in range(3))
+    hi = tuple(min(a[1][d], b[1][d]) for d in range(3))
+    return None if any(hi[d] < lo[d] for d in range(3)) else (lo, hi, tuple(a[2]))
+
+
+def reshape_counts(me, inboxes, outboxes):
+    """Elements rank `me` sends to / receives from every rank (rank order)."""
+    n = len(inboxes)
+    send = [0] * n
+    recv = [0] * n
+    for r in range(n):
+        o = collide(inboxes[me], outboxes[r]) if box_count(inboxes[me]) and box_count(outboxes[r]) else None
+        send[r] = box_count(o) if o else 0
+        o = collide(outboxes[me], inboxes[r]) if box_count(outboxes[me]) and box_count(inboxes[r]) else None
+        recv[r] = box_count(o) if o else 0
+    return send, recv
+
+
+def _offset_in(box, ov):
+    lo, _, order = box
+    return ((ov[0][order[2]] - lo[order[2]]) * _osize(box, 0) * _osize(box, 1) +
+            (ov[0][order[1]] - lo[order[1]]) * _osize(box, 0) + (ov[0][order[0]] - lo[order[0]]))
+
+
+def reshape_pack(me, inboxes, outboxes, data):
+    """The send buffer of rank `me`: the overlap of its input box with each
+    rank's output box, in rank order, each packed in the input box's order
+    (direct_pack, compute_overlap_map_direct_pack :147-167)."""
+    box = inboxes[me]
+    parts = []
+    for r in range(len(inboxes)):
+        o = collide(box, outboxes[r]) if box_count(box) and box_count(outboxes[r]) else None
+        if o is None:
+            continue
+        size = tuple(_osize(o, d) for d in range(3))
+        off = _offset_in(box, o)
+        parts.append(direct_pack(np.asarray(data)[off:], size, _osize(box, 0), _osize(box, 0) * _osize(box, 1)))
+    return np.concatenate(parts) if parts else np.zeros(0, np.asarray(data).dtype)
+
+
+def reshape_unpack(me, inboxes, outboxes, recv, out):
+    """Scatters rank `me`'s receive buffer (chunks in rank order, each in the
+    sender's input order) into its output box (transpose_unpack with the map
+    of compute_overlap_map_transpose_pack :197-222)."""
+    box = outboxes[me]
+    out = np.array(out, copy=True)
+    pos = 0
+    for r in range(len(inboxes)):
+        src = inboxes[r]
+        o = collide(box, src) if box_count(box) and box_count(src) else None
+        if o is None:
+            continue
+        size = tuple(_osize(o, d) for d in range(3))
+        mp = [0, 0, 0]
+        for j in range(3):
+            for k in range(3):
+                if box[2][k] == src[2][j]:
+                    mp[j] = k
+        n = box_count(o)
+        ext = [o[1][d] - o[0][d] + 1 for d in range(3)]
+        bls, bps = ext[src[2][0]], ext[src[2][0]] * ext[src[2][1]]
+        off = _offset_in(box, o)
+        view = out[off:]
+        view = transpose_unpack(recv[pos:pos + n], view, size, _osize(box, 0), _osize(box, 0) * _osize(box, 1),
+                                bls, bps, tuple(mp))
+        out[off:] = view
+        pos += n
+    return out
+
+
+def box_slice(global_canonical, box):
+    """The values of `box` (in its order) from an array indexed [k][j][i]."""
+    lo, hi, order = box
+    sub = global_canonical[lo[2]:hi[2] + 1, lo[1]:hi[1] + 1, lo[0]:hi[0] + 1]
+    return from_canonical(sub, order)
+
+
 def scale_data(x, factor, dtype):
     """data_scaling::apply: x *= (scalar)factor in the working precision."""
     x = np.asarray(x)
