@@ -425,8 +425,13 @@ def fp64_check(gb, box, x, stream, forms, kind="c2c"):
     import torch
     ref = fp64_host(kind, box.size, x)
     out = {}
+    single = x.dtype in (torch.float32, torch.complex64)
     for name, p in forms.items():
-        y = torch.empty(p.size_outbox(), dtype=torch.complex64 if kind != "cos" else torch.float32, device=x.device)
+        if kind == "cos":
+            odt = torch.float32 if single else torch.float64
+        else:
+            odt = torch.complex64 if single else torch.complex128
+        y = torch.empty(p.size_outbox(), dtype=odt, device=x.device)
         p.forward(x, y)
         out[name] = rel_l2_host(y, ref)
         del y
@@ -475,6 +480,9 @@ WORKLOADS = {
     "r2c512": ("r2c", (512, 512, 512), 0),
     "dct256": ("cos", (256, 256, 256), 0),
     "z2z512": ("c2c", (512, 512, 512), 1),
+    # the same with each arithmetic form of the complex<double> passes forced
+    "z2z512fp64": ("c2c", (512, 512, 512), 1, False, "fp64"),
+    "z2z512df": ("c2c", (512, 512, 512), 1, False, "double-float"),
     "c2c1024x1024x512": ("c2c", (1024, 1024, 512), 0),
     # the same two c2c float boxes with the radix-16 stages on the tensor cores
     "c2c512tc": ("c2c", (512, 512, 512), 0, True),
@@ -482,6 +490,12 @@ WORKLOADS = {
     # small case (256 MiB, above L2) for ncu captures of the tensor-core kernel
     "c2c512x512x128tc": ("c2c", (512, 512, 128), 0, True),
     "z2z64": ("c2c", (64, 64, 64), 1),
+    # small case (256 MiB complex<double>, above L2) for ncu captures of the FP64 pass kernels
+    "z2z256": ("c2c", (256, 256, 256), 1),
+    "z2z256fp64": ("c2c", (256, 256, 256), 1, False, "fp64"),
+    "z2z256df": ("c2c", (256, 256, 256), 1, False, "double-float"),
+    # the FP64 rate of this GPU: cuBLAS DGEMM 8192^3 through torch (burst)
+    "fp64peak": ("fp64peak", None, 1),
     # small case (256 MiB, above L2) for ncu captures of the c2c pass kernels
     "c2c512x512x128": ("c2c", (512, 512, 128), 0),
     # small case (256 MiB real input, above L2) for ncu captures of the r2c line pass
@@ -771,10 +785,38 @@ def run_location_workload(name, steps, warmup):
     return out
 
 
+def run_fp64_peak(name, steps, warmup):
+    """FP64 throughput of this GPU, the denominator of the complex<double>
+    transforms: cuBLAS DGEMM of 8192^3 through torch.matmul (2 n^3 flops per
+    product), best of `steps` timed products after `warmup`, CUDA events."""
+    import torch
+    n = 8192
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    a = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+    for _ in range(max(1, warmup)):
+        c = a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(max(1, steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del c
+    return {"workload": name, "method": "cuBLAS DGEMM 8192^3 (torch.matmul float64), best of %d" % max(1, steps),
+            "ms": best, "fp64_tflops": 2.0 * n ** 3 / (best / 1e3) / 1e12}
+
+
 def run_workload(name, steps, warmup):
     import torch
     import heffte_gb300 as gb
     kind, size, prec = WORKLOADS[name][:3]
+    if kind == "fp64peak":
+        return run_fp64_peak(name, steps, warmup)
     if kind == "selector":
         return run_selector_workload(name)
     if kind == "conv":
@@ -782,12 +824,28 @@ def run_workload(name, steps, warmup):
     if kind == "location":
         return run_location_workload(name, steps, warmup)
     tc = len(WORKLOADS[name]) > 3 and WORKLOADS[name][3]
+    arith = WORKLOADS[name][4] if len(WORKLOADS[name]) > 4 else None
+    if arith is not None:
+        old = gb.set_double_arithmetic(gb.FP64 if arith == "fp64" else gb.DOUBLE_FLOAT)
+        try:
+            out = run_workload_plain(name, steps, warmup, kind, size, prec, tc)
+        finally:
+            gb.set_double_arithmetic(old)
+        out["double_arithmetic"] = arith
+        return out
     if kind == "batch":
         cache = "loop" if size == "loop" else None
         if size == "tuned":
             import tempfile
             cache = os.path.join(tempfile.mkdtemp(), "tune.tsv")
         return run_batch_workload(name, steps, warmup, cache)
+    return run_workload_plain(name, steps, warmup, kind, size, prec, tc)
+
+
+def run_workload_plain(name, steps, warmup, kind, size, prec, tc):
+    """One transform workload (c2c / r2c / cos) timed over forward+backward steps."""
+    import torch
+    import heffte_gb300 as gb
     N = size[0] * size[1] * size[2]
     stream = torch.cuda.current_stream()
     box = gb.box3d((0, 0, 0), [s - 1 for s in size])
@@ -835,9 +893,8 @@ def run_workload(name, steps, warmup):
     peak, _ = peaks()
     out = {"workload": name, "ms_per_step": ms, "gflops": 2 * flops_per_transform(N) / (ms / 1e3) / 1e9,
            "gbs": b / (ms / 1e3) / 1e9, "hbm_frac": b / (ms / 1e3) / 1e9 / peak, "roundtrip_max_abs": err}
-    if prec == 0:
-        del y, z, work
-        out["rel_l2_forward_vs_fp64"] = fp64_check(gb, box, x, stream, {"p": plan}, kind)["p"]
+    del y, z, work
+    out["rel_l2_forward_vs_fp64"] = fp64_check(gb, box, x, stream, {"p": plan}, kind)["p"]
     if tc:
         out["tensor_cores"] = True
     return out

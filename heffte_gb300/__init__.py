@@ -485,6 +485,18 @@ def device_status(reset=False):
 
 DEV_TIMEOUT_BULK_COPY, DEV_TIMEOUT_DEPENDENCY, DEV_TIMEOUT_MMA = 1, 2, 3
 
+FP64, DOUBLE_FLOAT = 0, 1
+
+
+def set_double_arithmetic(mode):
+    """Arithmetic of the power-of-two complex<double> passes: FP64 (FP64
+    instructions) or DOUBLE_FLOAT (pairs of floats on the FP32 pipe); returns
+    the previous mode."""
+    old = lib().heffte_gb300_double_arithmetic()
+    check(lib().heffte_gb300_set_double_arithmetic(int(mode)))
+    return old
+
+
 
 def set_dependency_wait_budget(clocks):
     """Clock budget of the batch kernel's waits for another CTA's pass of the

@@ -70,6 +70,16 @@ int heffte_gb300_set_kernel_variant(int variant){
     });
 }
 
+int heffte_gb300_set_double_arithmetic(int mode){
+    return guard([&]{
+        if (mode != DA_FP64 && mode != DA_DOUBLE_FLOAT)
+            throw Error(ST_INVALID, "mode must be 0 (FP64 instructions) or 1 (double-float)");
+        set_double_arithmetic(mode);
+    });
+}
+
+int heffte_gb300_double_arithmetic(void){ return double_arithmetic(); }
+
 int heffte_gb300_device_status(int *status, int reset){
     return guard([&]{
         if (!status) throw Error(ST_INVALID, "null pointer");

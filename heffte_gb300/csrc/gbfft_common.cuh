@@ -6,10 +6,76 @@
 
 namespace gbfft {
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two
+// floats with |lo| <= ulp(hi) / 2 (about 48 significant bits), computed on
+// the FP32 pipe, which on GB300 issues 64 times the FP64 pipe's rate.  Built
+// from error-free transformations: Knuth's TwoSum, Dekker's FastTwoSum and
+// the FMA form of TwoProduct (Dekker 1971; the double-double operations of
+// Hida, Li and Bailey, 2001).  The sum is the normwise form (TwoSum of the
+// high parts, low parts added once): its error is bounded by about
+// 2^-46 (|a| + |b|), not by the size of the result, which is the bound the
+// normwise error analysis of an FFT uses.  The exponent range is the
+// float's: callers scale their data into it (the pipelined complex<double>
+// kernels scale each tile by a power of two).
+// ---------------------------------------------------------------------------
+struct __align__(8) df {
+    float hi, lo;
+    __host__ __device__ constexpr df() : hi(0.f), lo(0.f) {}
+    __host__ __device__ constexpr df(float h, float l) : hi(h), lo(l) {}
+    // constants of the butterflies (folded at compile time)
+    __host__ __device__ constexpr df(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+};
+
+__device__ __forceinline__ df df_two_sum(float a, float b){
+    float s = a + b;
+    float bb = s - a;
+    return df(s, (a - (s - bb)) + (b - bb));
+}
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ df df_fast_two_sum(float a, float b){
+    float s = a + b;
+    return df(s, b - (s - a));
+}
+__device__ __forceinline__ df operator+(df a, df b){
+    df s = df_two_sum(a.hi, b.hi);
+    return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ df operator-(df a){ return df(-a.hi, -a.lo); }
+__device__ __forceinline__ df operator-(df a, df b){ return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b){
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);          // exact low part of a.hi * b.hi
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ df &operator+=(df &a, df b){ a = a + b; return a; }
+__device__ __forceinline__ df &operator*=(df &a, df b){ a = a * b; return a; }
+// rounding conversions from / to double
+__device__ __forceinline__ df df_from(double x){
+    float hi = __double2float_rn(x);
+    return df(hi, __double2float_rn(x - (double)hi));
+}
+__device__ __forceinline__ double df_to(df a){ return (double)a.hi + (double)a.lo; }
+
+struct __align__(16) cdf { df x, y; };
+
 template<typename T> struct cplx;
 template<> struct cplx<float>  { using type = float2; };
 template<> struct cplx<double> { using type = double2; };
+template<> struct cplx<df>     { using type = cdf; };
 template<typename T> using c_t = typename cplx<T>::type;
+
+// read-only cached load of a complex value (twiddle tables)
+__device__ __forceinline__ float2 ldg_c(float2 const *p){ return __ldg(p); }
+__device__ __forceinline__ double2 ldg_c(double2 const *p){ return __ldg(p); }
+__device__ __forceinline__ cdf ldg_c(cdf const *p){
+    float4 v = __ldg(reinterpret_cast<float4 const*>(p));
+    cdf r;
+    r.x = df(v.x, v.y);
+    r.y = df(v.z, v.w);
+    return r;
+}
 
 template<typename T> __host__ __device__ __forceinline__ c_t<T> mk(T re, T im){ c_t<T> r; r.x = re; r.y = im; return r; }
 template<typename C> __device__ __forceinline__ C cadd(C a, C b){ C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }

@@ -40,6 +40,24 @@ __global__ void k_stockham_twiddles(Plan1D P, c_t<T> *tw){
     }
 }
 
+// the same table as double-float pairs: each FP64 value split into a
+// float and the float nearest to its remainder
+__global__ void k_stockham_twiddles_df(Plan1D P, cdf *tw){
+    for (int s = 1; s < P.nstages; s++){
+        Stage S = P.st[s];
+        int n = S.Ns * (S.R - 1);
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x){
+            int k = idx / (S.R - 1), q = idx % (S.R - 1) + 1;
+            double sn, cs;
+            sincospi(-2.0 * (double)(q * k) / (double)(S.Ns * S.R), &sn, &cs);
+            cdf w;
+            w.x = df_from(cs);
+            w.y = df_from(sn);
+            tw[S.tw + idx] = w;
+        }
+    }
+}
+
 template<typename T>
 __global__ void k_r2r_twiddles(int N, c_t<T> *tw){
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x){
@@ -68,6 +86,20 @@ void const *Fft1D::twiddles(int prec, cudaStream_t s){
         }
     }
     return tw[prec];
+}
+
+void const *Fft1D::twiddles_df(cudaStream_t s){
+    std::lock_guard<std::mutex> lk(mu);
+    if (!tw_df){
+        long long cnt = std::max<long long>(tw_count, 1);
+        check_cuda(cudaMalloc(&tw_df, cnt * sizeof(cdf)), "cudaMalloc(double-float twiddles)");
+        if (tw_count > 0){
+            int blocks = (int)std::min<long long>((tw_count + 255) / 256, 1024);
+            k_stockham_twiddles_df<<<blocks, 256, 0, s>>>(plan, reinterpret_cast<cdf*>(tw_df));
+            check_cuda(cudaPeekAtLastError(), "twiddle kernel");
+        }
+    }
+    return tw_df;
 }
 
 void const *Fft1D::r2r_twiddles(int prec, cudaStream_t s){
@@ -261,6 +293,10 @@ static std::atomic<int> g_variant{0};
 int kernel_variant(){ return g_variant.load(); }
 void set_kernel_variant(int v){ g_variant.store(v); }
 
+static std::atomic<int> g_double_arith{DA_FP64};
+int double_arithmetic(){ return g_double_arith.load(); }
+void set_double_arithmetic(int mode){ g_double_arith.store(mode); }
+
 int *device_status(){
     static int *ptrs[64] = {nullptr};
     static std::mutex mu;
@@ -383,6 +419,10 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
         if (c2c) return launch_pipe_f32_c2c(s, kind, f.N, cols, a);
         if (r2c) return launch_pipe_f32_r2c(s, kind, f.N, cols, a);
         return launch_pipe_f32_r2r(s, kind, f.N, cols, a);
+    }
+    if (c2c && double_arithmetic() == DA_DOUBLE_FLOAT){
+        a.tw = f.twiddles_df(s);
+        return launch_pipe_df64_c2c(s, kind, f.N, cols, a);
     }
     if (c2c) return launch_pipe_f64_c2c(s, kind, f.N, cols, a);
     if (r2c) return launch_pipe_f64_r2c(s, kind, f.N, cols, a);

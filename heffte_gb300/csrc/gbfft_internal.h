@@ -59,11 +59,14 @@ struct Fft1D {
     void *tw[2] = {nullptr, nullptr};     // Stockham twiddles
     void *rtw[2] = {nullptr, nullptr};    // exp(-i pi k / 2N), k < N (r2r)
     void *ctab[3][2] = {};                // composite tables (CompositeTable)
+    void *tw_df = nullptr;                // Stockham twiddles as double-float pairs
     long long tw_count = 0;
     std::mutex mu;
     ~Fft1D();
     void const *twiddles(int prec, cudaStream_t s);
     void const *r2r_twiddles(int prec, cudaStream_t s);
+    // the Stockham twiddles for double-float arithmetic (FP64-generated, split into float pairs)
+    void const *twiddles_df(cudaStream_t s);
     // four-step roots exp(-2 pi i m / N); Bluestein chirp exp(-i pi n^2 / N)
     // and the spectrum of its conjugate on M points divided by M (FP64-generated)
     void const *composite_table(int which, int prec, cudaStream_t s);
@@ -203,6 +206,8 @@ bool launch_pipe_f32_r2r(cudaStream_t s, int kind, int N, bool cols, PipeLaunch 
 bool launch_pipe_f64_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 bool launch_pipe_f64_r2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 bool launch_pipe_f64_r2r(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
+// complex<double> c2c passes in double-float arithmetic (a.tw: twiddles_df)
+bool launch_pipe_df64_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
 // Fused convolution pass (gbfft_conv.cuh): forward FFT of the columns of x
 // (and y), pointwise product, scale, backward FFT, in place in x.
 struct ConvLaunch {
@@ -234,6 +239,11 @@ std::vector<int> pipe_radices(int N);   // empty if N has no pipelined kernel
 // kernels only, 2 pipelined kernels wherever they apply.
 int kernel_variant();
 void set_kernel_variant(int v);
+// Arithmetic of the pipelined complex<double> c2c passes (process-wide):
+// 0 FP64 instructions, 1 double-float pairs on the FP32 pipe.
+enum { DA_FP64 = 0, DA_DOUBLE_FLOAT = 1 };
+int double_arithmetic();
+void set_double_arithmetic(int mode);
 
 // Per-device status word written by kernels whose bounded waits gave up.
 int *device_status();

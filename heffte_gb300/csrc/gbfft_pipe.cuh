@@ -161,7 +161,7 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
                 C const *w = tw + TWO + k * (R - 1);
                 #pragma unroll
                 for (int q = 1; q < R; q++){
-                    C wq = __ldg(w + q - 1);
+                    C wq = ldg_c(w + q - 1);
                     v[m * R + q] = FWD ? cmul(v[m * R + q], wq) : cmulc(v[m * R + q], wq);
                 }
             }
@@ -199,10 +199,13 @@ template<int NG> __device__ __forceinline__ void cp_async_wait(){ asm volatile("
 
 __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols){ return pipe_tpb(N, csize, cols) * pipe_tt(N); }
 
-template<typename T, int N, int KIND, bool COLS, int LOADER>
+// DF: complex<double> tiles transformed in double-float arithmetic (c2c kinds).
+template<typename T, int N, int KIND, bool COLS, int LOADER, bool DF = false>
 __global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS))
 k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
+    static_assert(!DF || ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && sizeof(T) == 8),
+                  "double-float arithmetic serves the complex<double> c2c kinds");
     constexpr bool PAIRED = pipe_paired(KIND);
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
     constexpr int TT = pipe_tt(N);
@@ -222,6 +225,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     C *tiles = reinterpret_cast<C*>(smraw);
     C *xline = tiles + NBUF * TILE;  // line tiles: padded exchange buffer
     __shared__ __align__(8) uint64_t bar[NBUF];
+    __shared__ unsigned s_emax[DF ? NT / 32 : 1];   // per-warp largest exponent of a tile (DF)
 
     int tid = threadIdx.x;
     int loc, t;
@@ -372,7 +376,55 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         int sine = P.sine;
         C v[16];
 
-        if constexpr (KIND == PK_C2C_FWD || KIND == PK_C2C_BWD){
+        if constexpr (DF){
+            // double-float: the tile is scaled by 2^-sh so that its largest
+            // magnitude lies in [1, 2) (the float exponent range then holds
+            // everything above 2^-126 of it; smaller values contribute less
+            // than 2^-126 of the tile's norm), transformed as float pairs, and
+            // scaled back by 2^sh (with the plan's scale) on the store
+            using D = c_t<df>;
+            uint4 const *words = reinterpret_cast<uint4 const*>(tb);
+            unsigned e = 0;
+            for (int i = tid; i < TILE; i += NT){
+                uint4 w = words[i];
+                e = max(e, max((w.y >> 20) & 0x7ffu, (w.w >> 20) & 0x7ffu));
+            }
+            e = __reduce_max_sync(0xffffffffu, e);
+            if (lane == 0) s_emax[warp] = e;
+            __syncthreads();
+            unsigned em = 0;
+            #pragma unroll
+            for (int w = 0; w < NT / 32; w++) em = max(em, s_emax[w]);
+            int sh = (em == 0) ? -1022 : (int)em - 1023;
+            sh = min(max(sh, -1022), 1022);
+            double const down = __hiloint2double((1023 - sh) << 20, 0);
+            double const up = __hiloint2double((1023 + sh) << 20, 0) * (P.do_scale ? P.scale : 1.0);
+            auto ld0 = [&](int p) -> D {
+                C v = COLS ? tb[p * TPB + loc] : tb[loc * N + p];
+                D r; r.x = df_from(v.x * down); r.y = df_from(v.y * down);
+                return r;
+            };
+            auto back = [&](D x) -> C { C r; r.x = df_to(x.x) * up; r.y = df_to(x.y) * up; return r; };
+            D *xd = reinterpret_cast<D*>(xch);
+            D const *twd = reinterpret_cast<D const*>(P.tw);
+            D vd[16];
+            C *out = reinterpret_cast<C*>(P.out);
+            if (!COLS && LOADER == LD_BULK && P.bulk_store){
+                auto st = [&](int p, D x){ tb[loc * N + p] = back(x); };
+                pstage<df, N, TPB, 0, FWD, COLS, false>(t, loc, xd, twd, vd, ld0, st);
+                fence_proxy_async_smem();
+                __syncthreads();
+                if (tid == 0){
+                    long long lines = ((long long)TPB < P.G - c0) ? (long long)TPB : (P.G - c0);
+                    bulk_s2g(out + base_of_fast(Lo, c0), tb, (uint32_t)(lines * N * sizeof(C)));
+                    bulk_commit();
+                }
+            } else {
+                auto st = [&](int p, D x){ if (va) out[oa + p * oes] = back(x); };
+                pstage<df, N, TPB, 0, FWD, COLS, false>(t, loc, xd, twd, vd, ld0, st);
+            }
+            (void)v;
+        } else if constexpr (KIND == PK_C2C_FWD || KIND == PK_C2C_BWD){
             auto ld0 = [&](int p) -> C { return COLS ? tb[p * TPB + loc] : tb[loc * N + p]; };
             C *out = reinterpret_cast<C*>(P.out);
             if (!COLS && LOADER == LD_BULK && P.bulk_store){

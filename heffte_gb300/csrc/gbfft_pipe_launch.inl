@@ -3,7 +3,11 @@
 //   GB_T          float or double
 //   GB_PIPE_NAME  the exported dispatcher
 //   GB_GROUP      0: c2c (forward, backward), 1: r2c + c2r, 2: r2r forward + backward
+//   GB_DF         1: complex<double> in double-float arithmetic (c2c group; default 0)
 // so that the instantiations compile in parallel.
+#ifndef GB_DF
+#define GB_DF 0
+#endif
 #include "gbfft_internal.h"
 #include "gbfft_pipe.cuh"
 #include <atomic>
@@ -73,7 +77,7 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }
-    auto kern = k_pipe<T, N, KIND, COLS, LOADER>;
+    auto kern = k_pipe<T, N, KIND, COLS, LOADER, GB_DF != 0>;
     static std::atomic<unsigned long long> ready{0};
     static int blocks_per_sm[64] = {0};
     int dev = 0;

@@ -68,6 +68,18 @@ int heffte_gb300_version(void);
  * kernels only, 2 pipelined kernels wherever they apply. */
 int heffte_gb300_set_kernel_variant(int variant);
 
+/* No reference counterpart.  Arithmetic of the complex<double> passes of
+ * power-of-two lengths (the pipelined kernels) for all later calls of this
+ * process: 0 = FP64 instructions; 1 = double-float, each value carried as
+ * the unevaluated sum of two floats (about 48 significant bits) on the FP32
+ * pipe, every tile scaled by a power of two into the float exponent range
+ * (values below 2^-126 of a tile's largest are dropped, which changes the
+ * tile's norm by less than 2^-126).  Both hold rel-L2 <= 1e-12 against an
+ * FP64 transform; on GB300 the FP64 pipe issues 1/64 of the FP32 rate.
+ * Other lengths and kinds always use FP64 instructions. */
+int heffte_gb300_set_double_arithmetic(int mode);
+int heffte_gb300_double_arithmetic(void);
+
 /* No reference counterpart.  Reads the current device's status word: 0 = no
  * fault; otherwise a bounded device wait gave up and its kernel returned
  * early, so that call's output is invalid: 1 = a wait for a bulk (TMA) copy,
