@@ -51,12 +51,90 @@ __device__ __forceinline__ df operator*(df a, df b){
 }
 __device__ __forceinline__ df &operator+=(df &a, df b){ a = a + b; return a; }
 __device__ __forceinline__ df &operator*=(df &a, df b){ a = a * b; return a; }
-// rounding conversions from / to double
+// rounding conversions from / to double (FP64 instructions; for tables)
 __device__ __forceinline__ df df_from(double x){
     float hi = __double2float_rn(x);
     return df(hi, __double2float_rn(x - (double)hi));
 }
 __device__ __forceinline__ double df_to(df a){ return (double)a.hi + (double)a.lo; }
+
+// Bit casts usable on host and device (the conversions below are checked
+// bit for bit on the host).
+__host__ __device__ __forceinline__ uint64_t bits_of(double x){
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b; __builtin_memcpy(&b, &x, 8); return b;
+#endif
+}
+__host__ __device__ __forceinline__ double double_of(uint64_t b){
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double x; __builtin_memcpy(&x, &b, 8); return x;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t bits_of(float x){
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__float_as_uint(x);
+#else
+    uint32_t b; __builtin_memcpy(&b, &x, 4); return b;
+#endif
+}
+__host__ __device__ __forceinline__ float float_of(uint32_t b){
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float x; __builtin_memcpy(&x, &b, 4); return x;
+#endif
+}
+
+// x * 2^-sh as a float pair without FP64 instructions (integer and FP32
+// operations only; the FP64 pipe of GB300 issues 1/64 of the FP32 rate).
+// The 53-bit significand M is split into its nearest 24-bit head H (hi, exact)
+// and the signed remainder M - H 2^29 (|r| <= 2^28, rounded once to a float:
+// lo).  Scaled values below the float normal range (2^-126) are returned as
+// zero, and so are zeros and subnormal doubles.  sh must make the scaled
+// value < 2^128 (the kernels choose it from the tile's largest exponent).
+__host__ __device__ __forceinline__ df df_from_scaled(double x, int sh){
+    uint64_t b = bits_of(x);
+    uint32_t const sign = (uint32_t)(b >> 32) & 0x80000000u;
+    int const e = (int)((b >> 52) & 0x7ff);
+    int ef = e - sh - 896;                        // float biased exponent of the scaled value
+    if (e == 0 || ef <= 0) return df(0.f, 0.f);
+    uint64_t const M = (b & 0xfffffffffffffull) | (1ull << 52);
+    uint64_t H = (M + (1ull << 28)) >> 29;        // 2^23 <= H <= 2^24
+    int const r = (int)((int64_t)M - (int64_t)(H << 29));
+    // lo = r 2^(ef - 179), the power split so both factors are normal floats
+    float lo = (float)r * float_of((uint32_t)(ef - 79 + 127) << 23) * float_of((uint32_t)(-100 + 127) << 23);
+    if (H == (1ull << 24)){ H >>= 1; ef += 1; }
+    float const hi = float_of(sign | ((uint32_t)ef << 23) | ((uint32_t)H & 0x7fffffu));
+    return df(hi, sign ? -lo : lo);
+}
+
+// float -> double bits by widening (exact); 0 for zero, ~0 for a subnormal
+// float (the caller takes its slow path then)
+__host__ __device__ __forceinline__ uint64_t widen_bits(float f){
+    uint32_t const b = bits_of(f);
+    uint32_t const e = (b >> 23) & 0xffu;
+    if ((b & 0x7fffffffu) == 0) return (uint64_t)(b & 0x80000000u) << 32;
+    if (e == 0 || e == 0xffu) return ~0ull;
+    return ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
+}
+
+// (hi + lo) * 2^sh as a double with a single FP64 instruction (the sum of
+// the two exactly widened floats); the power of two is an exponent addition,
+// or a multiplication where the result would leave the normal range.
+__host__ __device__ __forceinline__ double df_to_scaled(df a, int sh){
+    uint64_t const h = widen_bits(a.hi), l = widen_bits(a.lo);
+    double const p2 = double_of((uint64_t)(1023 + sh) << 52);     // 2^sh, |sh| <= 1022
+    if (h == ~0ull || l == ~0ull) return ((double)a.hi + (double)a.lo) * p2;
+    double const s = double_of(h) + double_of(l);
+    uint64_t const sb = bits_of(s);
+    int const E = (int)((sb >> 52) & 0x7ff);
+    if (E == 0 || E + sh <= 0 || E + sh >= 2047) return s * p2;
+    return double_of(sb + ((uint64_t)(int64_t)sh << 52));
+}
 
 struct __align__(16) cdf { df x, y; };
 

@@ -324,6 +324,9 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         if (tl < P.ntiles) issue(tl, i);
     }
     T sc = (T)P.scale;
+    // the plan's scale as a float pair (double-float tiles)
+    df scale_df;
+    if constexpr (DF) scale_df = df_from(P.scale);
     for (int it = 0; tile < P.ntiles; tile += gridDim.x, it++){
         int b = it % NBUF;
         // the tile NBUF - 1 ahead goes into the buffer consumed last iteration
@@ -397,14 +400,18 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             for (int w = 0; w < NT / 32; w++) em = max(em, s_emax[w]);
             int sh = (em == 0) ? -1022 : (int)em - 1023;
             sh = min(max(sh, -1022), 1022);
-            double const down = __hiloint2double((1023 - sh) << 20, 0);
-            double const up = __hiloint2double((1023 + sh) << 20, 0) * (P.do_scale ? P.scale : 1.0);
+            // the conversions use integer and FP32 instructions (one FP64
+            // addition per value on the way back), see df_from_scaled
             auto ld0 = [&](int p) -> D {
                 C v = COLS ? tb[p * TPB + loc] : tb[loc * N + p];
-                D r; r.x = df_from(v.x * down); r.y = df_from(v.y * down);
+                D r; r.x = df_from_scaled(v.x, sh); r.y = df_from_scaled(v.y, sh);
                 return r;
             };
-            auto back = [&](D x) -> C { C r; r.x = df_to(x.x) * up; r.y = df_to(x.y) * up; return r; };
+            auto back = [&](D x) -> C {
+                if (P.do_scale){ x.x = x.x * scale_df; x.y = x.y * scale_df; }
+                C r; r.x = df_to_scaled(x.x, sh); r.y = df_to_scaled(x.y, sh);
+                return r;
+            };
             D *xd = reinterpret_cast<D*>(xch);
             D const *twd = reinterpret_cast<D const*>(P.tw);
             D vd[16];

@@ -496,15 +496,21 @@ def port_pack(op, src, dst, size, ls, ps, bls=0, bps=0, mp=(0, 1, 2)):
 
 
 def rel_l2(a, b, chunk=1 << 24):
-    """||a - b|| / ||b|| in float64, in chunks (full-size boxes hold 2^29 values)."""
+    """||a - b|| / ||b|| in float64, in chunks (full-size boxes hold 2^29
+    values), both scaled by the largest |b| so that squares of magnitudes near
+    the float64 limits neither overflow nor underflow."""
     a = np.asarray(a).ravel()
     b = np.asarray(b).ravel()
     assert a.size == b.size, (a.size, b.size)
     dt = np.complex128 if np.iscomplexobj(a) or np.iscomplexobj(b) else np.float64
+    m = 0.0
+    for i in range(0, b.size, chunk):
+        m = max(m, float(np.max(np.abs(b[i:i + chunk].astype(dt)))) if b[i:i + chunk].size else 0.0)
+    m = m if m > 0 and np.isfinite(m) else 1.0
     num = den = 0.0
     for i in range(0, a.size, chunk):
-        ai = a[i:i + chunk].astype(dt)
-        bi = b[i:i + chunk].astype(dt)
+        ai = a[i:i + chunk].astype(dt) / m
+        bi = b[i:i + chunk].astype(dt) / m
         num += float(np.sum(np.abs(ai - bi) ** 2))
         den += float(np.sum(np.abs(bi) ** 2))
     return float(np.sqrt(num) / (np.sqrt(den) if den > 0 else 1.0))
