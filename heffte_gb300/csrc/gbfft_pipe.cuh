@@ -68,8 +68,17 @@ __host__ __device__ constexpr int pipe_pe(int N){ return (N < 16) ? N : 16; }   
 __host__ __device__ constexpr int pipe_tt(int N){ return N / pipe_pe(N); }        // threads per unit
 __host__ __device__ constexpr int pipe_padn(int N){ return N + N / 16 + 1; }
 __host__ __device__ constexpr bool pipe_paired(int kind){ return kind >= PK_R2C_FWD; }
-// units (complex transforms or real pairs) per tile
-__host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols){
+// units (complex transforms or real pairs) per tile.  df: the double-float
+// complex<double> kernels, which are bound by the latency of their FP32
+// dependency chains rather than by memory: CTAs of about 128 threads and two
+// tile slots (at most ~100 KB of shared memory) so that two or three CTAs
+// share an SM and more warps hide that latency.
+__host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols, bool df = false){
+    if (df){
+        int tpb = (128 / pipe_tt(N) > 1) ? 128 / pipe_tt(N) : 1;
+        while (tpb > 1 && 2 * (N + 4) * tpb * csize + (cols ? 0 : tpb * pipe_padn(N) * csize) > 100 * 1024) tpb /= 2;
+        return tpb;
+    }
     int tt = pipe_tt(N);
     int tpb = cols ? ((csize == 8) ? 16 : 8) : 1;
     if (cols){ while (tpb * tt < 256 && tpb < 256) tpb *= 2; }
@@ -94,14 +103,14 @@ __host__ __device__ constexpr int pipe_tile_elems(int N, int tpb, int kind){
 // column tiles of the tensor-map loader whose two buffers already take more
 // than half of an SM's shared memory (one CTA per SM, so a deeper prefetch is
 // what keeps more copies in flight), two otherwise.
-__host__ __device__ constexpr int pipe_nbuf(int N, int csize, bool cols, int kind, int loader){
-    return (cols && loader == LD_TENSOR && (kind == PK_C2C_FWD || kind == PK_C2C_BWD) &&
+__host__ __device__ constexpr int pipe_nbuf(int N, int csize, bool cols, int kind, int loader, bool df = false){
+    return (!df && cols && loader == LD_TENSOR && (kind == PK_C2C_FWD || kind == PK_C2C_BWD) &&
             2 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize > 114 * 1024 &&
             3 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize <= 200 * 1024) ? 3 : 2;
 }
-__host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind, int loader){
-    int tpb = pipe_tpb(N, csize, cols);
-    return pipe_nbuf(N, csize, cols, kind, loader) * pipe_tile_elems(N, tpb, kind) * csize +
+__host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind, int loader, bool df = false){
+    int tpb = pipe_tpb(N, csize, cols, df);
+    return pipe_nbuf(N, csize, cols, kind, loader, df) * pipe_tile_elems(N, tpb, kind) * csize +
            (cols ? 0 : tpb * pipe_padn(N) * csize);
 }
 
@@ -197,17 +206,19 @@ __device__ __forceinline__ void cp_async_16(void *dst, void const *src, bool val
 __device__ __forceinline__ void cp_async_commit(){ asm volatile("cp.async.commit_group;" ::: "memory"); }
 template<int NG> __device__ __forceinline__ void cp_async_wait(){ asm volatile("cp.async.wait_group %0;" :: "n"(NG) : "memory"); }
 
-__host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols){ return pipe_tpb(N, csize, cols) * pipe_tt(N); }
+__host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool df = false){
+    return pipe_tpb(N, csize, cols, df) * pipe_tt(N);
+}
 
 // DF: complex<double> tiles transformed in double-float arithmetic (c2c kinds).
 template<typename T, int N, int KIND, bool COLS, int LOADER, bool DF = false>
-__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS))
+__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, DF))
 k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
     static_assert(!DF || ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && sizeof(T) == 8),
                   "double-float arithmetic serves the complex<double> c2c kinds");
     constexpr bool PAIRED = pipe_paired(KIND);
-    constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
+    constexpr int TPB = pipe_tpb(N, sizeof(C), COLS, DF);
     constexpr int TT = pipe_tt(N);
     constexpr int NT = TPB * TT;
     constexpr int TILE = pipe_tile_elems(N, TPB, KIND);   // complex elements per buffer
@@ -218,7 +229,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     constexpr int WIDTH = PAIRED ? 2 * TPB : TPB;           // input elements per tile row (columns)
     constexpr bool FWD = (KIND == PK_C2C_FWD || KIND == PK_R2C_FWD || KIND == PK_R2R_FWD);
     constexpr int PADN = pipe_padn(N);
-    constexpr int NBUF = pipe_nbuf(N, (int)sizeof(C), COLS, KIND, LOADER);
+    constexpr int NBUF = pipe_nbuf(N, (int)sizeof(C), COLS, KIND, LOADER, DF);
     static_assert(LOADER != LD_CPASYNC || NBUF == 2, "cp.async tiles are double buffered");
 
     extern __shared__ __align__(128) unsigned char smraw[];

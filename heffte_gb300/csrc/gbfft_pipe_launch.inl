@@ -22,10 +22,11 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     using T = GB_T;
     using C = c_t<T>;
     constexpr bool PAIRED = pipe_paired(KIND);
-    constexpr int TPB = pipe_tpb(N, sizeof(C), COLS);
-    constexpr int SMEM = pipe_smem(N, sizeof(C), COLS, KIND, LOADER);
+    constexpr bool DF = GB_DF != 0;
+    constexpr int TPB = pipe_tpb(N, sizeof(C), COLS, DF);
+    constexpr int SMEM = pipe_smem(N, sizeof(C), COLS, KIND, LOADER, DF);
     static_assert(SMEM <= 227 * 1024, "pipelined tile exceeds the shared memory of a CTA");
-    constexpr int THREADS = pipe_threads(N, sizeof(C), COLS);
+    constexpr int THREADS = pipe_threads(N, sizeof(C), COLS, DF);
     constexpr int IN_ES = (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD || KIND == PK_R2R_BWD) ? (int)sizeof(T) : (int)sizeof(C);
     constexpr int ROWS = (KIND == PK_C2R_BWD) ? N / 2 + 1 : N;
     constexpr int WIDTH = PAIRED ? 2 * TPB : TPB;
@@ -77,7 +78,7 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }
-    auto kern = k_pipe<T, N, KIND, COLS, LOADER, GB_DF != 0>;
+    auto kern = k_pipe<T, N, KIND, COLS, LOADER, DF>;
     static std::atomic<unsigned long long> ready{0};
     static int blocks_per_sm[64] = {0};
     int dev = 0;
