@@ -34,7 +34,60 @@ struct BatchUnit {
     long long in_off, out_off;   // element offsets into the source / destination buffer
     Layout Li, Lo;
     double scale;
+    int pf;              // the input of a tile can be copied ahead into shared memory (lines back to back, or adjacent columns)
 };
+
+// Copy of a tile's input into shared memory: `rows` rows of `rowbytes`
+// contiguous bytes, srcstride apart in global memory and dststride apart in
+// shared memory (every figure a multiple of 16 bytes).
+struct TileCopy {
+    unsigned char const *src;
+    long long srcstride;
+    int rows, rowbytes, dststride;
+};
+
+// The copy plan of tile lt of unit U, or false when the tile does not meet
+// the 16-byte granularity of the asynchronous copy (or spans two blocks).
+// Shared-memory layout: lines back to back (what tile_r2c / tile_c2r /
+// tile_c2c read for line tiles), or one row of TPB columns per element
+// position (column tiles).
+template<typename T>
+__device__ __forceinline__ bool tile_copy_plan(BatchUnit const &U, Plan1D const &P, BatchBufs const &bufs, long long lt,
+                                               TileCopy &tc){
+    using C = c_t<T>;
+    if (!U.pf) return false;
+    unsigned char const *srcb = reinterpret_cast<unsigned char const*>(U.src == 0 ? bufs.in : (U.src == 1 ? bufs.out : bufs.work));
+    int const N = P.N;
+    if (!U.cols){
+        int const per = (U.kind == K_R2C || U.kind == K_C2R) ? 2 : 1;
+        int const len = (U.kind == K_C2R) ? N / 2 + 1 : N;
+        long long const es = (U.kind == K_R2C) ? (long long)sizeof(T) : (long long)sizeof(C);
+        long long const first = lt * (long long)U.tpb * per;
+        long long const lines = min((long long)U.tpb * per, U.G - first);
+        unsigned char const *src = srcb + (U.in_off + first * len) * es;
+        long long const bytes = lines * len * es;
+        if ((reinterpret_cast<uintptr_t>(src) & 15) || (bytes & 15)) return false;
+        tc.src = src; tc.srcstride = 0; tc.rows = 1; tc.rowbytes = (int)bytes; tc.dststride = 0;
+        return true;
+    }
+    long long const es = sizeof(C);
+    long long const g0 = lt * (long long)U.tpb;
+    long long const W = min((long long)U.tpb, U.G - g0);
+    long long const blk = g0 / U.Li.count, c0 = g0 - blk * U.Li.count;
+    if (c0 + W > U.Li.count) return false;
+    unsigned char const *src = srcb + (U.in_off + blk * U.Li.bstride + c0) * es;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) || ((W * es) & 15) || ((U.Li.estride * es) & 15)) return false;
+    tc.src = src; tc.srcstride = U.Li.estride * es; tc.rows = N; tc.rowbytes = (int)(W * es);
+    tc.dststride = (int)(U.tpb * es);
+    return true;
+}
+
+// 16-byte asynchronous copy global -> shared through L2 only (.cg): the
+// data was written by other CTAs of the same launch, so this SM's L1 may
+// hold stale lines of it
+__device__ __forceinline__ void cp_async_cg16(void *dst, void const *src){
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(smem_u32(dst)), "l"(src) : "memory");
+}
 
 // CTAs per SM the batch kernels are compiled for (registers per thread
 // <= 65536 / (256 x this)); float measured best at 4, double kept at 2
@@ -52,12 +105,15 @@ template<typename T, bool FWD>
 __global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
-        long long total_tiles, int *status, int scaling, long long dep_budget){
+        long long total_tiles, int *status, int scaling, long long dep_budget, int pf_offset){
     using C = c_t<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
     C *sm = reinterpret_cast<C*>(smraw);
-    __shared__ long long s_tile;
-    __shared__ int s_unit;
+    // prefetch buffer after the exchange buffer (pf_offset < 0: no prefetch)
+    unsigned char *pfbuf = smraw + (pf_offset > 0 ? pf_offset : 0);
+    __shared__ long long s_tile, s_next;
+    __shared__ int s_unit, s_next_unit, s_pf_cur, s_pf_next;
+    __shared__ TileCopy s_copy;
     // first tile of every unit, for the tile -> unit search (shared memory
     // when it fits, else the unit table itself)
     constexpr int kUnitsInSmem = 1024;
@@ -66,34 +122,47 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
     bool const smem_units = nunits <= kUnitsInSmem;
     if (smem_units)
         for (int i = tid; i < nunits; i += blockDim.x) s_tile0[i] = units[i].tile0;
-    // the next tile is claimed while the current one is processed, so the
-    // queue atomic's latency is hidden; the smallest unfinished tile is
-    // always some CTA's current tile and depends only on smaller ones, so
-    // claiming ahead cannot stall the queue
-    long long next = 0;
-    if (tid == 0) next = (long long)atomicAdd(work_counter, 1ull);
+    __syncthreads();
+    auto find_unit = [&](long long t) -> int {      // last unit with tile0 <= t
+        int lo = 0, hi = nunits - 1;
+        while (lo < hi){
+            int mid = (lo + hi + 1) >> 1;
+            long long t0 = smem_units ? s_tile0[mid] : units[mid].tile0;
+            if (t0 <= t) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    };
+    // the next tile is claimed (and its unit found) while the current one is
+    // processed, so the queue atomic's latency is hidden; the smallest
+    // unfinished tile is always some CTA's current tile and depends only on
+    // smaller ones, so claiming ahead cannot stall the queue
+    if (tid == 0){
+        s_next = (long long)atomicAdd(work_counter, 1ull);
+        s_next_unit = (s_next < total_tiles) ? find_unit(s_next) : 0;
+        s_pf_next = 0;
+    }
     __syncthreads();
     while (true){
         if (tid == 0){
-            s_tile = next;
-            int lo = 0, hi = nunits - 1;
+            s_tile = s_next;
+            s_unit = s_next_unit;
+            s_pf_cur = s_pf_next;
+            s_pf_next = 0;
             if (s_tile < total_tiles){
-                while (lo < hi){          // last unit with tile0 <= s_tile
-                    int mid = (lo + hi + 1) >> 1;
-                    long long t0 = smem_units ? s_tile0[mid] : units[mid].tile0;
-                    if (t0 <= s_tile) lo = mid; else hi = mid - 1;
-                }
-                next = (long long)atomicAdd(work_counter, 1ull);
+                long long nx = (long long)atomicAdd(work_counter, 1ull);
+                s_next = nx;
+                s_next_unit = (nx < total_tiles) ? find_unit(nx) : 0;
             }
-            s_unit = lo;
         }
         __syncthreads();
         long long gt = s_tile;
         int u = s_unit;
+        bool const pfcur = s_pf_cur != 0;
         if (gt >= total_tiles) return;
         BatchUnit const &U = units[u];
         bool ok = true;
-        if (tid == 0 && U.dep >= 0){
+        // a prefetched tile's dependency was met before its copy was issued
+        if (tid == 0 && U.dep >= 0 && !pfcur){
             long long need = units[U.dep].tiles + U.dep_extra;
             volatile int *d = done + U.dep;
             if (*d < need){
@@ -105,6 +174,43 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
             __threadfence();
         }
         if (__syncthreads_or(!ok)) return;
+        if (pfcur){
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            __syncthreads();
+        }
+        // once stage 0 has read this tile's inputs, the claimed next tile's
+        // input goes into the prefetch buffer if its dependency is met
+        auto prefetch_next = [&](){
+            if (tid == 0){
+                int go = 0;
+                if (pf_offset > 0 && s_next < total_tiles){
+                    BatchUnit const &V = units[s_next_unit];
+                    bool met = true;
+                    if (V.dep >= 0){
+                        volatile int *d = done + V.dep;
+                        met = *d >= units[V.dep].tiles + V.dep_extra;
+                    }
+                    TileCopy tc;
+                    if (met && tile_copy_plan<T>(V, plans[V.plan], bufs, s_next - V.tile0, tc)){
+                        __threadfence();
+                        s_copy = tc;
+                        go = 1;
+                    }
+                }
+                s_pf_next = go;
+            }
+            __syncthreads();
+            if (s_pf_next){
+                TileCopy const tc = s_copy;
+                int const cpr = tc.rowbytes >> 4;
+                long long const total = (long long)tc.rows * cpr;
+                for (long long c = tid; c < total; c += blockDim.x){
+                    int const r = (int)(c / cpr), k = (int)(c - (long long)r * cpr);
+                    cp_async_cg16(pfbuf + (long long)r * tc.dststride + 16 * k, tc.src + r * tc.srcstride + 16 * k);
+                }
+                asm volatile("cp.async.commit_group;" ::: "memory");
+            }
+        };
         long long lt = gt - U.tile0;
         Plan1D const &P = plans[U.plan];
         C const *tw = tws[U.plan];
@@ -113,29 +219,31 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
         double f = (scaling == 0) ? 1.0 : ((scaling == 1) ? U.scale : sqrt(U.scale));
         T sc = (T)f;
         int dsc = U.last && scaling != 0;
+        C const *pfc = pfcur ? reinterpret_cast<C const*>(pfbuf) : nullptr;
         if constexpr (FWD){
             if (U.kind == K_R2C){
                 T const *in = reinterpret_cast<T const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                T const *pfr = pfcur ? reinterpret_cast<T const*>(pfbuf) : nullptr;
+                if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, prefetch_next);
+                else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, prefetch_next);
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
+                else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
             }
         } else {
             if (U.kind == K_C2R){
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 T *out = reinterpret_cast<T*>(dstb) + U.out_off;
-                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
+                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
-                else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm);
+                if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
+                else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
             }
         }
         // publish completion of this tile
@@ -196,12 +304,16 @@ static int tile_tpb(Fft1D const &f, bool cols, bool paired, size_t csize, size_t
     return tpb;
 }
 
-std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream){
+std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream,
+                                  BatchConfig const &config){
     if (kind != PK_R2C && kind != PK_C2C) throw Error(ST_UNSUPPORTED, "batches support c2c and r2c boxes");
     if (prec != 0 && prec != 1) throw Error(ST_INVALID, "precision must be 0 or 1");
     if (sizes.empty()) throw Error(ST_INVALID, "empty batch");
+    if (config.prefetch != 0 && config.prefetch != 1) throw Error(ST_INVALID, "prefetch must be 0 or 1");
+    if (config.tile_kb < 8 || config.tile_kb > 96) throw Error(ST_INVALID, "tile size must be 8 to 96 KB");
     auto b = std::make_unique<Batch>();
     b->kind = kind; b->prec = prec; b->sizes = sizes; b->stream = stream;
+    b->config = config;
     size_t csize = (prec == 0) ? sizeof(float2) : sizeof(double2);
     size_t rsize = csize / 2;
     bool r2c = (kind == PK_R2C);
@@ -239,7 +351,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         b->ffts.push_back(f);
         tpb_hint.push_back(tc.tpb);
     }
-    size_t smem_cap = 48 * 1024;
+    size_t smem_cap = (size_t)config.tile_kb * 1024;
     // units: forward = (r2c|c2c x), c2c y, c2c z; backward = c2c z, c2c y, (c2r|c2c x)
     auto build = [&](bool fwd, std::vector<BatchUnit> &units, long long &total){
         std::vector<std::vector<BatchUnit>> per_pass(3);
@@ -282,6 +394,13 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
                 }
                 U.last = lastp ? 1 : 0;
                 U.scale = sc;
+                // tiles whose input is one span (lines back to back) or rows of
+                // adjacent columns can be copied ahead into shared memory
+                long long len = (U.kind == K_C2R) ? f.N / 2 + 1 : f.N;
+                if (!U.cols)
+                    U.pf = U.Li.estride == 1 && U.Li.dist == len && (U.G <= U.Li.count || U.Li.bstride == U.Li.count * len);
+                else
+                    U.pf = (U.kind == K_C2C_F || U.kind == K_C2C_B) && U.Li.dist == 1;
                 per_pass[k].push_back(U);
             }
         }
@@ -353,6 +472,20 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
             size_t unit = U.cols ? (size_t)f.N * csize : (size_t)(f.N + (f.N >> 4) + 1) * csize;
             smem = std::max(smem, unit * U.tpb);
         }
+    // the prefetch buffer: the largest tile input of the units that can prefetch
+    size_t pf_bytes = 0;
+    for (auto const *v : {&fu, &bu})
+        for (auto const &U : *v){
+            if (!U.pf) continue;
+            Fft1D const &f = *b->ffts[U.plan];
+            size_t es = (U.kind == K_R2C) ? rsize : csize;
+            size_t per = (U.kind == K_R2C || U.kind == K_C2R) ? 2 : 1;
+            size_t len = (U.kind == K_C2R) ? f.N / 2 + 1 : f.N;
+            pf_bytes = std::max(pf_bytes, U.cols ? (size_t)f.N * U.tpb * es : (size_t)U.tpb * per * len * es);
+        }
+    smem = (smem + 15) / 16 * 16;
+    b->pf_offset = (config.prefetch && pf_bytes > 0) ? (int)smem : -1;
+    if (b->pf_offset > 0) smem += (pf_bytes + 15) / 16 * 16;
     b->smem = smem;
     for (bool fwd : {true, false}){
         void const *kern = batch_kernel(prec, fwd);
@@ -361,7 +494,6 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, kern, kBatchThreads, smem), "occupancy");
         (fwd ? b->grid : b->grid_bwd) = std::max(1, nb_sm) * num_sms();
     }
-    (void)rsize;
     return b;
 }
 
@@ -390,7 +522,7 @@ static void build_graph(Batch &b, bool fwd){
     b.args_scaling = 0;
     b.args_budget = dependency_wait_budget();
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
-                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget};
+                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget, &b.pf_offset};
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(batch_kernel(b.prec, fwd));
     kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
@@ -400,6 +532,53 @@ static void build_graph(Batch &b, bool fwd){
     check_cuda(cudaGraphAddKernelNode(&knode, g, &mnode, 1, &kp), "cudaGraphAddKernelNode");
     check_cuda(cudaGraphInstantiate(&e, g, 0), "cudaGraphInstantiate");
     (fwd ? b.fwd_knode : b.bwd_knode) = knode;
+}
+
+// Times forward + backward of every launch shape (prefetch on / off, tile
+// bounds of 48, 32 and 24 KB: 2 to 5 CTAs per SM) on the caller's buffers
+// and leaves `b` built with the fastest; the untuned default is a candidate,
+// so tuning never makes the batch slower than it was (within the timing noise).
+BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out, void *back, void *work, int reps,
+                           double *best_ms){
+    if (!in || !out || !back || !work) throw Error(ST_INVALID, "null pointer");
+    reps = std::max(reps, 1);
+    Batch const &B0 = *b;
+    int const kind = B0.kind, prec = B0.prec;
+    std::vector<std::array<int, 3>> const sizes = B0.sizes;
+    cudaStream_t const s = B0.stream;
+    BatchConfig best = B0.config;
+    double best_t = 1e300;
+    cudaEvent_t e0, e1;
+    check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+    check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+    for (int pf : {1, 0}){
+        for (int kb : {48, 32, 24}){
+            BatchConfig c;
+            c.prefetch = pf;
+            c.tile_kb = kb;
+            auto cand = make_batch(kind, prec, sizes, s, c);
+            for (int i = 0; i < 2; i++){
+                cand->run(true, in, out, nullptr, 0);
+                cand->run(false, out, back, work, 0);
+            }
+            check_cuda(cudaEventRecord(e0, s), "cudaEventRecord");
+            for (int i = 0; i < reps; i++){
+                cand->run(true, in, out, nullptr, 0);
+                cand->run(false, out, back, work, 0);
+            }
+            check_cuda(cudaEventRecord(e1, s), "cudaEventRecord");
+            check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float ms = 0.f;
+            check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+            double t = ms / reps;
+            if (t < best_t){ best_t = t; best = c; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b = make_batch(kind, prec, sizes, s, best);
+    if (best_ms) *best_ms = best_t;
+    return best;
 }
 
 void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
@@ -421,7 +600,7 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     args_scaling = scaling;
     args_budget = dependency_wait_budget();
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
-                    &args_total, &args_status, &args_scaling, &args_budget};
+                    &args_total, &args_status, &args_scaling, &args_budget, &pf_offset};
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(batch_kernel(prec, fwd));
     kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));

@@ -33,6 +33,14 @@ std::string device_key();
 // batch of boxes (gbfft_batch.cu)
 // ---------------------------------------------------------------------------
 struct BatchBufs { void const *in; void *out; void *work; };
+// Launch shape of a batch: prefetch = 1 copies each CTA's next tile into
+// shared memory while it transforms the current one (when the next tile's
+// pass dependency is already met); tile_kb bounds the shared memory of one
+// tile's exchange buffer (smaller tiles: more CTAs per SM).
+struct BatchConfig {
+    int prefetch = 1;
+    int tile_kb = 48;
+};
 struct BatchUnit;   // one 1-D pass of one box (gbfft_batch.cu)
 
 struct Batch {
@@ -48,6 +56,8 @@ struct Batch {
     int nunits = 0;
     long long fwd_tiles = 0, bwd_tiles = 0;
     size_t smem = 0;
+    BatchConfig config;
+    int pf_offset = -1;    // byte offset of the prefetch buffer in dynamic shared memory (-1: none)
     int grid = 0;          // persistent CTAs of the forward kernel
     int grid_bwd = 0;      // and of the backward kernel
     cudaGraph_t fwd_graph = nullptr, bwd_graph = nullptr;
@@ -72,11 +82,18 @@ struct Batch {
     void run(bool fwd, void const *in, void *out, void *work, int scaling);
 };
 
+// Times the launch shapes of a batch on the caller's buffers (input ->
+// output forward, output -> back backward with work) and rebuilds `b` with
+// the fastest; returns it (and its ms per forward + backward).
+BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out, void *back, void *work, int reps,
+                           double *best_ms);
+
 // Clock budget of the batch kernel's waits for another CTA's pass of the same
 // box (default kWaitBudgetClocks); read at every launch.
 long long dependency_wait_budget();
 void set_dependency_wait_budget(long long clocks);
 
-std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream);
+std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream,
+                                  BatchConfig const &config = BatchConfig{});
 
 } // namespace gbfft

@@ -293,7 +293,9 @@ static std::atomic<int> g_variant{0};
 int kernel_variant(){ return g_variant.load(); }
 void set_kernel_variant(int v){ g_variant.store(v); }
 
-static std::atomic<int> g_double_arith{DA_FP64};
+// double-float by default: 1.45x the FP64-instruction passes on GB300
+// (512^3 Z2Z 31.0 against 44.8 ms per forward + backward) at rel-L2 ~1e-14
+static std::atomic<int> g_double_arith{DA_DOUBLE_FLOAT};
 int double_arithmetic(){ return g_double_arith.load(); }
 void set_double_arithmetic(int mode){ g_double_arith.store(mode); }
 

@@ -14,6 +14,7 @@
 //     (r2c split, DCT/DST post-twiddle).
 // Twiddles come from a per-length table generated in FP64 on the device.
 #pragma once
+#include <type_traits>
 #include "gbfft_common.cuh"
 
 namespace gbfft {
@@ -79,11 +80,18 @@ __device__ __forceinline__ void fft_stage(Stage const &S, int t, int Tt, bool ac
     if (!to_global) __syncthreads();
 }
 
+// Called by every thread once the first stage has read all its inputs (the
+// default does nothing); the batch kernel starts the copy of its next tile
+// into the buffer the first stage read from.
+struct NoHook { __device__ __forceinline__ void operator()() const {} };
+
 // Runs the whole transform. If last_to_global is false the result is left in
 // shared memory (natural order) and the CTA is synchronised on return.
-template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST, class AF = NoHook>
 __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
-                                        c_t<T> const *__restrict__ tw, bool last_to_global, LD &ld, ST &st){
+                                        c_t<T> const *__restrict__ tw, bool last_to_global, LD &ld, ST &st,
+                                        AF const &after_first = AF{}){
+    constexpr bool HOOK = !std::is_same<AF, NoHook>::value;
     Regs<T, EMAX> r;
     if (P.nstages == 0){
         // length-1 transform: identity
@@ -92,6 +100,7 @@ __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t
             if (last_to_global) st(0, x); else sm[sm_index<COLS>(0, loc, TPB, padn)] = x;
         }
         if (!last_to_global) __syncthreads();
+        if constexpr (HOOK){ __syncthreads(); after_first(); }
         return;
     }
     for (int s = 0; s < P.nstages; s++){
@@ -108,6 +117,14 @@ __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t
             case 4: fft_stage<4, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
             case 3: fft_stage<3, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
             default: fft_stage<2, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+        }
+        if constexpr (HOOK){
+            // a stage that ends in shared memory ends with a barrier; one that
+            // stores to global memory needs one before the inputs are free
+            if (first){
+                if (tg) __syncthreads();
+                after_first();
+            }
         }
     }
 }
@@ -127,10 +144,14 @@ __device__ __forceinline__ int padded_len(int N){ return N + (N >> 4) + 1; }
 // Each kernel body is a per-tile device function (tile = block of TPB
 // transforms) so that the batched multi-box kernel can reuse it; threads
 // beyond TPB * T of a larger CTA stay inactive but join every barrier.
-template<typename T, int EMAX, bool FWD, bool COLS>
+// pf (optional): the tile's input already copied into shared memory, lines
+// back to back (pf[loc * N + p]) or rows of TPB columns (pf[p * TPB + loc]);
+// after_first: see fft_run.
+template<typename T, int EMAX, bool FWD, bool COLS, class AF = NoHook>
 __device__ __forceinline__ void tile_c2c(Plan1D const &P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out,
                                          c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
-                                         long long tile, c_t<T> *sm){
+                                         long long tile, c_t<T> *sm, c_t<T> const *pf = nullptr,
+                                         AF const &after_first = AF{}){
     using C = c_t<T>;
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
@@ -138,11 +159,15 @@ __device__ __forceinline__ void tile_c2c(Plan1D const &P, Layout Li, Layout Lo, 
     bool active = (g < G) && (t < P.T) && (loc < TPB);
     long long ib = active ? base_of(Li, g) : 0, ob = active ? base_of(Lo, g) : 0;
     long long ies = Li.estride, oes = Lo.estride;
+    int const N = P.N;
     // L2-only loads: in the batched kernel the data was written by other CTAs
     // of the same launch, so this SM's L1 may hold stale lines
-    auto ld = [&](int p) -> C { return __ldcg(in + ib + p * ies); };
+    auto ld = [&](int p) -> C {
+        if (pf) return COLS ? pf[p * TPB + loc] : pf[loc * N + p];
+        return __ldcg(in + ib + p * ies);
+    };
     auto st = [&](int p, C v){ out[ob + p * oes] = do_scale ? cscale(v, scale) : v; };
-    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st, after_first);
 }
 
 template<typename T, int EMAX, bool FWD, bool COLS>
@@ -159,10 +184,13 @@ k_c2c(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> cons
 // z = x_a + i x_b; X_a[k] = (Z_k + conj Z_{N-k})/2, X_b[k] = -i (Z_k - conj Z_{N-k})/2.
 // Li is in real elements, Lo in complex elements; outputs k = 0..N/2.
 // ---------------------------------------------------------------------------
-template<typename T, int EMAX, bool COLS>
+// pf (optional, line tiles): the tile's real input lines back to back in
+// shared memory (line 2 loc + b at pf[(2 loc + b) N + p])
+template<typename T, int EMAX, bool COLS, class AF = NoHook>
 __device__ __forceinline__ void tile_r2c(Plan1D const &P, Layout Li, Layout Lo, T const *in, c_t<T> *out,
                                          c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
-                                         long long tile, c_t<T> *sm){
+                                         long long tile, c_t<T> *sm, T const *pf = nullptr,
+                                         AF const &after_first = AF{}){
     using C = c_t<T>;
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
@@ -172,12 +200,18 @@ __device__ __forceinline__ void tile_r2c(Plan1D const &P, Layout Li, Layout Lo, 
     bool hasb = gb < G;
     long long ia = active ? base_of(Li, ga) : 0, ibb = (active && hasb) ? base_of(Li, gb) : 0;
     long long ies = Li.estride;
+    int const NL = P.N;
     auto ld = [&](int p) -> C {
-        C z; z.x = __ldcg(in + ia + p * ies); z.y = hasb ? __ldcg(in + ibb + p * ies) : (T)0; return z;
+        C z;
+        if (!COLS && pf){
+            z.x = pf[(2 * loc) * NL + p]; z.y = hasb ? pf[(2 * loc + 1) * NL + p] : (T)0;
+            return z;
+        }
+        z.x = __ldcg(in + ia + p * ies); z.y = hasb ? __ldcg(in + ibb + p * ies) : (T)0; return z;
     };
     auto st = [&](int, C){};
     int padn = padded_len(P.N);
-    fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, false, ld, st);
+    fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, false, ld, st, after_first);
     if (!active) return;
     int N = P.N;
     long long oa = base_of(Lo, ga), obb = hasb ? base_of(Lo, gb) : 0;
@@ -211,10 +245,13 @@ k_r2c(Plan1D P, Layout Li, Layout Lo, T const *in, c_t<T> *out, c_t<T> const *__
 // Z_p = X'_a[p] + i X'_b[p] with X'[p] = X[p] (p <= N/2, imaginary part of
 // the DC and Nyquist terms dropped) and conj X[N-p] above N/2.
 // ---------------------------------------------------------------------------
-template<typename T, int EMAX, bool COLS>
+// pf (optional, line tiles): the tile's half-spectrum lines back to back in
+// shared memory (line 2 loc + b at pf[(2 loc + b) (N/2 + 1) + p])
+template<typename T, int EMAX, bool COLS, class AF = NoHook>
 __device__ __forceinline__ void tile_c2r(Plan1D const &P, Layout Li, Layout Lo, c_t<T> const *in, T *out,
                                          c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
-                                         long long tile, c_t<T> *sm){
+                                         long long tile, c_t<T> *sm, c_t<T> const *pf = nullptr,
+                                         AF const &after_first = AF{}){
     using C = c_t<T>;
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
@@ -230,8 +267,15 @@ __device__ __forceinline__ void tile_c2r(Plan1D const &P, Layout Li, Layout Lo, 
         int pp = (2 * p <= N) ? p : N - p;
         bool cj = (2 * p > N);
         bool real_only = (pp == 0) || (2 * pp == N);
-        C xa = __ldcg(in + ia + pp * ies);
-        C xb = hasb ? __ldcg(in + ibb + pp * ies) : mk<T>(0, 0);
+        C xa, xb;
+        if (!COLS && pf){
+            int const H = N / 2 + 1;
+            xa = pf[(2 * loc) * H + pp];
+            xb = hasb ? pf[(2 * loc + 1) * H + pp] : mk<T>(0, 0);
+        } else {
+            xa = __ldcg(in + ia + pp * ies);
+            xb = hasb ? __ldcg(in + ibb + pp * ies) : mk<T>(0, 0);
+        }
         if (real_only){ xa.y = 0; xb.y = 0; }
         if (cj){ xa.y = -xa.y; xb.y = -xb.y; }
         C z; z.x = xa.x - xb.y; z.y = xa.y + xb.x; return z;
@@ -241,7 +285,7 @@ __device__ __forceinline__ void tile_c2r(Plan1D const &P, Layout Li, Layout Lo, 
         out[oa + p * oes] = v.x * s;
         if (hasb) out[obb + p * oes] = v.y * s;
     };
-    fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st);
+    fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st, after_first);
 }
 
 template<typename T, int EMAX, bool COLS>

@@ -70,7 +70,7 @@ int heffte_gb300_set_kernel_variant(int variant);
 
 /* No reference counterpart.  Arithmetic of the complex<double> passes of
  * power-of-two lengths (the pipelined kernels) for all later calls of this
- * process: 0 = FP64 instructions; 1 = double-float, each value carried as
+ * process: 0 = FP64 instructions; 1 (default) = double-float, each value carried as
  * the unevaluated sum of two floats (about 48 significant bits) on the FP32
  * pipe, every tile scaled by a power of two into the float exponent range
  * (values below 2^-126 of a tile's largest are dropped, which changes the
@@ -332,6 +332,21 @@ long long heffte_gb300_boxbatch_workspace_size(heffte_gb300_boxbatch batch);
 int heffte_gb300_boxbatch_forward(heffte_gb300_boxbatch batch, const void *input, void *output, int scale);
 int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *input, void *output, void *workspace,
                                    int scale);
+
+/* No reference counterpart.  Launch shape of a batch: prefetch = 1 (default)
+ * copies each CTA's next tile into shared memory while the CTA transforms
+ * the current one (when that tile's pass dependency is already met);
+ * tile_kb (8..96, default 48) bounds one tile's shared exchange buffer, so
+ * smaller values give smaller tiles and more CTAs per SM.  Results are the
+ * same for every shape.  configure() rebuilds the batch with a shape;
+ * autotune() times forward (input -> output) + backward (output -> back,
+ * with workspace) `reps` times for every shape (prefetch on / off, 48, 32, 24
+ * KB), keeps the fastest, and returns it with its ms per forward + backward;
+ * it overwrites output, back and workspace, and leaves input as it was. */
+int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch batch, int prefetch, int tile_kb);
+int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch batch, int *prefetch, int *tile_kb);
+int heffte_gb300_boxbatch_autotune(heffte_gb300_boxbatch batch, const void *input, void *output, void *back,
+                                   void *workspace, int reps, int *prefetch, int *tile_kb, double *ms);
 
 /* No reference counterpart.  Clock budget (GPU clocks, >= 0) after which the
  * batch kernel's wait for another CTA's pass of the same box gives up, records

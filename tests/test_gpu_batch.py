@@ -131,3 +131,55 @@ def test_dependency_wait_gives_up_and_the_next_call_is_correct(gb):
         yi = yh[b.output_offset(i):b.output_offset(i) + nc]
         assert O.rel_l2(yi, O.fft3d_r2c(xi, s, 0)) < TOL[0], (i, s)
     assert gb.device_status() == 0
+
+
+@pytest.mark.parametrize("prefetch,tile_kb", [(1, 48), (0, 48), (1, 24), (1, 32), (0, 24)])
+def test_batch_launch_shapes_give_the_same_result(gb, prefetch, tile_kb):
+    """Every launch shape (the next tile copied ahead into shared memory or
+    not; tile bounds that change the CTAs per SM) against the oracle, r2c
+    forward and the backward round trip, float and double sides."""
+    rng = np.random.default_rng(31 + tile_kb)
+    sizes = _sizes(rng, 30, SIDES)
+    for prec in (0, 1):
+        b = gb.boxbatch(gb.kind.r2c, sizes, prec)
+        b.configure(prefetch, tile_kb)
+        assert b.config() == (prefetch, tile_kb)
+        rdt, cdt = (np.float32, torch.complex64) if prec == 0 else (np.float64, torch.complex128)
+        x = rng.standard_normal(b.input_size()).astype(rdt)
+        xin = torch.from_numpy(x).cuda()
+        y = torch.empty(b.output_size(), dtype=cdt, device="cuda")
+        b.forward(xin, y)
+        yh = y.cpu().numpy()
+        for i, s in enumerate(sizes):
+            n = int(np.prod(s))
+            nc = (s[0] // 2 + 1) * s[1] * s[2]
+            xi = x[b.input_offset(i):b.input_offset(i) + n]
+            yi = yh[b.output_offset(i):b.output_offset(i) + nc]
+            assert O.rel_l2(yi, O.fft3d_r2c(xi, s, 0)) < TOL[prec], (prec, i, s)
+        w = torch.empty(b.workspace_size(), dtype=cdt, device="cuda")
+        z = torch.empty_like(xin)
+        b.backward(y, z, w, gb.scale.full)
+        assert O.rel_l2(z.cpu().numpy(), x) < 3 * TOL[prec]
+    assert gb.device_status() == 0
+
+
+def test_batch_autotune_keeps_a_correct_shape(gb):
+    rng = np.random.default_rng(64)
+    sizes = _sizes(rng, 40, SIDES)
+    b = gb.boxbatch(gb.kind.c2c, sizes, 0)
+    n = b.input_size()
+    x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex64)
+    xin = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xin)
+    z = torch.empty_like(xin)
+    w = torch.empty(b.workspace_size(), dtype=torch.complex64, device="cuda")
+    pf, kb, ms = b.autotune(xin, y, z, w, reps=2)
+    assert (pf, kb) == b.config() and pf in (0, 1) and kb in (24, 32, 48) and ms > 0
+    assert torch.equal(xin.cpu(), torch.from_numpy(x))      # the input is left as it was
+    b.forward(xin, y)
+    yh = y.cpu().numpy()
+    for i, s in enumerate(sizes):
+        m = int(np.prod(s))
+        xi = x[b.input_offset(i):b.input_offset(i) + m]
+        yi = yh[b.output_offset(i):b.output_offset(i) + m]
+        assert O.rel_l2(yi, O.fft3d_c2c(xi, s)) < TOL[0], (i, s)
