@@ -76,7 +76,11 @@ __device__ __forceinline__ bool tile_copy_plan(BatchUnit const &U, Plan1D const 
     long long const blk = g0 / U.Li.count, c0 = g0 - blk * U.Li.count;
     if (c0 + W > U.Li.count) return false;
     unsigned char const *src = srcb + (U.in_off + blk * U.Li.bstride + c0) * es;
-    if ((reinterpret_cast<uintptr_t>(src) & 15) || ((W * es) & 15) || ((U.Li.estride * es) & 15)) return false;
+    // both sides of every 16-byte copy aligned: the source start and row
+    // stride, the row length, and the shared-memory row stride (TPB columns)
+    if ((reinterpret_cast<uintptr_t>(src) & 15) || ((W * es) & 15) || ((U.Li.estride * es) & 15) ||
+        (((long long)U.tpb * es) & 15))
+        return false;
     tc.src = src; tc.srcstride = U.Li.estride * es; tc.rows = N; tc.rowbytes = (int)(W * es);
     tc.dststride = (int)(U.tpb * es);
     return true;
