@@ -399,7 +399,11 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             using D = c_t<df>;
             uint4 const *words = reinterpret_cast<uint4 const*>(tb);
             unsigned e = 0;
-            for (int i = tid; i < TILE; i += NT){
+            // only the tile's own lines: the line loader copies the last,
+            // partial tile's lines alone, and the rows past them still hold
+            // an older tile (column tiles are zero-filled past the edge)
+            int const scan = COLS ? TILE : (int)min((long long)TILE, (P.G - c0) * N);
+            for (int i = tid; i < scan; i += NT){
                 uint4 w = words[i];
                 e = max(e, max((w.y >> 20) & 0x7ffu, (w.w >> 20) & 0x7ffu));
             }
