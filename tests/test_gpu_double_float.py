@@ -94,23 +94,23 @@ def test_double_float_partial_last_tile(double_float):
     the tile buffer, and the rows past them still hold an earlier tile's values
     (here 2^300 larger), which must not set the last tile's scale.  The 1-D
     executor along dimension 0 of 64 x 255 x 129 (32895 lines: several tiles
-    per CTA, a partial last one), the first half of the lines 2^300 larger;
-    every line of the small half against the FP64 oracle, each on its own
-    scale.  And a single line (a one-line tile), as Bluestein's chirp
+    per CTA, a partial last one), the first 16384 lines (whole tiles of any
+    power-of-two width) 2^300 larger; every other line against the FP64
+    oracle, each on its own scale.  And a single line (a one-line tile), as Bluestein's chirp
     spectrum is computed."""
     gb = double_float
     size = (64, 255, 129)
     lines = size[1] * size[2]
     rng = np.random.default_rng(77)
     x = rng.uniform(-1, 1, (lines, size[0])) + 1j * rng.uniform(-1, 1, (lines, size[0]))
-    x[:lines // 2] *= 2.0 ** 300
+    x[:16384] *= 2.0 ** 300
     ex = gb.executor(gb.kind.c2c, gb.box3d((0, 0, 0), [s - 1 for s in size]), [0])
     xin = torch.from_numpy(x.reshape(-1)).cuda()
     y = torch.empty_like(xin)
     ex.forward(1, xin, y)
     torch.cuda.synchronize()
-    got = y.cpu().numpy().reshape(lines, size[0])[lines // 2:]
-    want = np.fft.fft(x[lines // 2:], axis=1)
+    got = y.cpu().numpy().reshape(lines, size[0])[16384:]
+    want = np.fft.fft(x[16384:], axis=1)
     err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
     assert err.max() < TOL, (int(err.argmax()), err.max())
     one = rng.uniform(-1, 1, 64) + 1j * rng.uniform(-1, 1, 64)
