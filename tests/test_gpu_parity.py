@@ -304,21 +304,14 @@ def test_r2c_sizes_against_fp64(gb, size, prec):
                 assert np.array_equal(host(y), yh), "c2r modified its input"
 
 
-def _smooth13(n):
-    for q in (2, 3, 5, 7, 11, 13):
-        while n % q == 0:
-            n //= q
-    return n == 1
-
-
 @pytest.mark.parametrize("size", [(8, 8, 8), (7, 6, 5), (16, 9, 4), (1, 5, 3), (32, 24, 20), (33, 25, 17),
                                   (65, 9, 2), (257, 129, 65)])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("rkind", [2, 3, 4])
 def test_r2r_sizes_against_fp64(gb, size, prec, rkind):
-    # DCT-I of n values runs on an FFT of length 2(n - 1)
-    ok_len = (lambda n: n >= 2 and _smooth13(2 * (n - 1))) if rkind == 4 else _smooth13
-    if not all(ok_len(n) for n in size):
+    # every length runs (lengths with a prime factor above 13 through
+    # Bluestein's algorithm); DCT-I of n values needs n >= 2
+    if rkind == 4 and min(size) < 2:
         with pytest.raises(gb.HeffteError):
             gb.rtransform(rkind, gb.box3d((0, 0, 0), [s - 1 for s in size]),
                           gb.box3d((0, 0, 0), [s - 1 for s in size]))
