@@ -27,27 +27,53 @@ struct __align__(8) df {
     __host__ __device__ constexpr df(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
 };
 
-__device__ __forceinline__ df df_two_sum(float a, float b){
+// A rounded product that the compiler may not contract with a later addition
+// into one FMA (the error-free transformations need the rounded value).
+__host__ __device__ __forceinline__ float mul_rn(float a, float b){
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+
+__host__ __device__ __forceinline__ df df_two_sum(float a, float b){
     float s = a + b;
     float bb = s - a;
     return df(s, (a - (s - bb)) + (b - bb));
 }
 // |a| >= |b| (or a == 0)
-__device__ __forceinline__ df df_fast_two_sum(float a, float b){
+__host__ __device__ __forceinline__ df df_fast_two_sum(float a, float b){
     float s = a + b;
     return df(s, b - (s - a));
 }
-__device__ __forceinline__ df operator+(df a, df b){
+__host__ __device__ __forceinline__ df operator+(df a, df b){
     df s = df_two_sum(a.hi, b.hi);
     return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
 }
-__device__ __forceinline__ df operator-(df a){ return df(-a.hi, -a.lo); }
-__device__ __forceinline__ df operator-(df a, df b){ return a + (-b); }
-__device__ __forceinline__ df operator*(df a, df b){
-    float p = a.hi * b.hi;
+__host__ __device__ __forceinline__ df operator-(df a){ return df(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ df operator-(df a, df b){ return a + (-b); }
+__host__ __device__ __forceinline__ df operator*(df a, df b){
+    float p = mul_rn(a.hi, b.hi);
     float e = fmaf(a.hi, b.hi, -p);          // exact low part of a.hi * b.hi
     e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
     return df_fast_two_sum(p, e);
+}
+// a * b + c * d, renormalised once (the twiddle products of the FFT stages):
+// the two head products summed exactly, the low-order terms added once; the
+// error is bounded by about 2^-45 (|a b| + |c d|), the normwise bound
+__host__ __device__ __forceinline__ df df_dot2(df a, df b, df c, df d){
+    float const p1 = mul_rn(a.hi, b.hi), p2 = mul_rn(c.hi, d.hi);
+    float const e1 = fmaf(a.hi, b.hi, -p1), e2 = fmaf(c.hi, d.hi, -p2);
+    float const s = p1 + p2;
+    float const bb = s - p1;
+    float e = ((p1 - (s - bb)) + (p2 - bb)) + (e1 + e2);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    e = fmaf(c.hi, d.lo, e);
+    e = fmaf(c.lo, d.hi, e);
+    float const h = s + e;
+    return df(h, e - (h - s));
 }
 __device__ __forceinline__ df &operator+=(df &a, df b){ a = a + b; return a; }
 __device__ __forceinline__ df &operator*=(df &a, df b){ a = a * b; return a; }
@@ -166,6 +192,13 @@ template<typename C> __device__ __forceinline__ C cmulc(C a, C b){
     C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
 }
 template<typename C> __device__ __forceinline__ C cconj(C a){ C r; r.x = a.x; r.y = -a.y; return r; }
+// double-float complex products through the fused dot (one renormalisation per part)
+__host__ __device__ __forceinline__ cdf cmul(cdf a, cdf b){
+    cdf r; r.x = df_dot2(a.x, b.x, -a.y, b.y); r.y = df_dot2(a.x, b.y, a.y, b.x); return r;
+}
+__host__ __device__ __forceinline__ cdf cmulc(cdf a, cdf b){
+    cdf r; r.x = df_dot2(a.x, b.x, a.y, b.y); r.y = df_dot2(a.y, b.x, -a.x, b.y); return r;
+}
 // multiply by -i (forward) or +i (backward)
 template<bool FWD, typename C> __device__ __forceinline__ C rot90(C a){
     C r;
