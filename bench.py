@@ -504,8 +504,10 @@ WORKLOADS = {
     "batch256": ("batch", None, 0),
     # the same after autotuning the radix plan / tile size of every side length
     "batch256tuned": ("batch", "tuned", 0),
-    # the same without the prefetch of each CTA's next tile (the earlier form)
-    "batch256noprefetch": ("batch", "noprefetch", 0),
+    # the same with each CTA's next tile copied ahead into shared memory
+    "batch256prefetch": ("batch", "prefetch", 0),
+    # the same queued in groups of 16 MB of boxes, each group's passes two groups apart (L2-resident)
+    "batch256grouped": ("batch", "grouped", 0),
     # the same boxes as a loop over one fft3d_r2c plan per box (how the reference runs them)
     "batch256loop": ("batch", "loop", 0),
     # learned plan selection on the 2000 measured shapes (tests/golden/selector_timings.npz)
@@ -581,8 +583,9 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     stream = torch.cuda.current_stream()
     if tune_cache == "loop":
         return run_batch_loop(name, sizes, steps, warmup)
-    noprefetch = tune_cache == "noprefetch"
-    if noprefetch:
+    # launch shapes other than the default (prefetch, tile KB, group MB)
+    fixed = {"prefetch": (1, 48, 0), "grouped": (0, 48, 16)}.get(tune_cache)
+    if fixed:
         tune_cache = None
     plans = None
     if tune_cache is not None:
@@ -592,8 +595,8 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
             rad, tpb, us = gb.tuned_choice(0, n)
             plans[str(n)] = {"radices": rad, "tpb": tpb, "us_per_tuning_batch": us}
     b = gb.boxbatch(gb.kind.r2c, sizes, 0, stream=stream)
-    if noprefetch:
-        b.configure(prefetch=0, tile_kb=48)
+    if fixed:
+        b.configure(*fixed)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(7)
     x = torch.randn(b.input_size(), device="cuda", generator=gen)
@@ -603,9 +606,9 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
 
     shape = None
     if tune_cache is not None:
-        # the launch shape (prefetch, tile bound) timed on these buffers
-        pf, kb, tms = b.autotune(x, y, z, w, reps=5)
-        shape = {"prefetch": pf, "tile_kb": kb, "ms_at_tuning": tms}
+        # the launch shape (prefetch, tile bound, queue groups) timed on these buffers
+        pf, kb, gm, tms = b.autotune(x, y, z, w, reps=5)
+        shape = {"prefetch": pf, "tile_kb": kb, "group_mb": gm, "ms_at_tuning": tms}
 
     def step():
         b.forward(x, y, gb.scale.full)
@@ -628,7 +631,7 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     return {"workload": name, "boxes": len(sizes), "ms_per_step": ms, "gflops": flops / (ms / 1e3) / 1e9,
             "gbs": byts / (ms / 1e3) / 1e9, "hbm_frac": byts / (ms / 1e3) / 1e9 / peak,
             "roundtrip_max_abs": err, "launches_per_step": 2, "tuned": tune_cache is not None,
-            "launch_shape": dict(zip(("prefetch", "tile_kb"), b.config())),
+            "launch_shape": dict(zip(("prefetch", "tile_kb", "group_mb"), b.config())),
             **({"tuned_plans": plans} if plans else {}), **({"tuned_shape": shape} if shape else {})}
 
 
@@ -848,7 +851,7 @@ def run_workload(name, steps, warmup):
         out["double_arithmetic"] = arith
         return out
     if kind == "batch":
-        cache = size if size in ("loop", "noprefetch") else None
+        cache = size if size in ("loop", "prefetch", "grouped") else None
         if size == "tuned":
             import tempfile
             cache = os.path.join(tempfile.mkdtemp(), "tune.tsv")

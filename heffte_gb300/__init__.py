@@ -104,10 +104,12 @@ def lib():
     L.heffte_gb300_set_dependency_wait_budget.argtypes = [ll]
     L.heffte_gb300_dependency_wait_budget.restype = ll
     L.heffte_gb300_boxbatch_hold_dependencies.argtypes = [vp, i]
-    L.heffte_gb300_boxbatch_configure.argtypes = [vp, i, i]
-    L.heffte_gb300_boxbatch_config.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.heffte_gb300_boxbatch_configure.argtypes = [vp, i, i, i]
+    L.heffte_gb300_boxbatch_config.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                               ctypes.POINTER(ctypes.c_int)]
     L.heffte_gb300_boxbatch_autotune.argtypes = [vp, vp, vp, vp, vp, i, ctypes.POINTER(ctypes.c_int),
-                                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+                                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                 ctypes.POINTER(ctypes.c_double)]
     L.heffte_gb300_boxbatch_forward.argtypes = [vp, vp, vp, i]
     L.heffte_gb300_boxbatch_backward.argtypes = [vp, vp, vp, vp, i]
     L.heffte_gb300_tune.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_int)]
@@ -542,23 +544,25 @@ class boxbatch:
     def workspace_size(self):
         return lib().heffte_gb300_boxbatch_workspace_size(self._h)
 
-    def configure(self, prefetch=1, tile_kb=48):
-        """Launch shape: prefetch of each CTA's next tile, tile bound in KB."""
-        check(lib().heffte_gb300_boxbatch_configure(self._h, int(prefetch), int(tile_kb)))
+    def configure(self, prefetch=0, tile_kb=48, group_mb=0):
+        """Launch shape: prefetch of each CTA's next tile, tile bound in KB,
+        queue order (boxes in L2-sized groups of group_mb MB, 0: pass-major)."""
+        check(lib().heffte_gb300_boxbatch_configure(self._h, int(prefetch), int(tile_kb), int(group_mb)))
 
     def config(self):
-        pf, kb = ctypes.c_int(0), ctypes.c_int(0)
-        check(lib().heffte_gb300_boxbatch_config(self._h, ctypes.byref(pf), ctypes.byref(kb)))
-        return pf.value, kb.value
+        pf, kb, gm = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        check(lib().heffte_gb300_boxbatch_config(self._h, ctypes.byref(pf), ctypes.byref(kb), ctypes.byref(gm)))
+        return pf.value, kb.value, gm.value
 
     def autotune(self, inarray, outarray, back, workspace, reps=5):
         """Times every launch shape on these buffers (forward in -> out,
         backward out -> back) and keeps the fastest; returns (prefetch,
-        tile_kb, ms per forward + backward)."""
-        pf, kb, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        tile_kb, group_mb, ms per forward + backward)."""
+        pf, kb, gm, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
         check(lib().heffte_gb300_boxbatch_autotune(self._h, _ptr(inarray), _ptr(outarray), _ptr(back), _ptr(workspace),
-                                                   int(reps), ctypes.byref(pf), ctypes.byref(kb), ctypes.byref(ms)))
-        return pf.value, kb.value, ms.value
+                                                   int(reps), ctypes.byref(pf), ctypes.byref(kb), ctypes.byref(gm),
+                                                   ctypes.byref(ms)))
+        return pf.value, kb.value, gm.value, ms.value
 
     def hold_dependencies(self, hold):
         """Test hook: every pass dependency waits for a tile that never comes

@@ -105,6 +105,14 @@ template<typename T> constexpr int batch_ctas_per_sm(){ return sizeof(T) == 4 ? 
 // few spills cost (256 uneven r2c float boxes, ms per step: 2.09 at one CTA
 // per SM, 1.54 at two, 1.46 at three, 1.38 at four, 1.64-1.80 at five to
 // eight).
+// the stage-0 hook of the batch kernel: on only when the batch prefetches
+template<class F> struct PrefetchHook {
+    F const &f;
+    bool on;
+    __device__ __forceinline__ bool enabled() const { return on; }
+    __device__ __forceinline__ void operator()() const { f(); }
+};
+
 template<typename T, bool FWD>
 __global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
@@ -215,6 +223,7 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 asm volatile("cp.async.commit_group;" ::: "memory");
             }
         };
+        PrefetchHook<decltype(prefetch_next)> const hook{prefetch_next, pf_offset > 0};
         long long lt = gt - U.tile0;
         Plan1D const &P = plans[U.plan];
         C const *tw = tws[U.plan];
@@ -229,25 +238,25 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 T const *in = reinterpret_cast<T const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
                 T const *pfr = pfcur ? reinterpret_cast<T const*>(pfbuf) : nullptr;
-                if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, prefetch_next);
-                else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, prefetch_next);
+                if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
+                else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
-                else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
+                if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
             }
         } else {
             if (U.kind == K_C2R){
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 T *out = reinterpret_cast<T*>(dstb) + U.out_off;
-                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
-                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
+                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
-                else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, prefetch_next);
+                if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
             }
         }
         // publish completion of this tile
@@ -315,6 +324,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     if (sizes.empty()) throw Error(ST_INVALID, "empty batch");
     if (config.prefetch != 0 && config.prefetch != 1) throw Error(ST_INVALID, "prefetch must be 0 or 1");
     if (config.tile_kb < 8 || config.tile_kb > 96) throw Error(ST_INVALID, "tile size must be 8 to 96 KB");
+    if (config.group_mb < 0 || config.group_mb > 4096) throw Error(ST_INVALID, "group size must be 0 to 4096 MB");
     auto b = std::make_unique<Batch>();
     b->kind = kind; b->prec = prec; b->sizes = sizes; b->stream = stream;
     b->config = config;
@@ -412,19 +422,46 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         total = 0;
         int nb = (int)sizes.size();
         std::vector<int> pos(3 * nb);      // pos[k * nb + box] = unit index of pass k of box
-        for (int k = 0; k < 3; k++){
-            // larger boxes first within a pass (balances the tail)
-            std::vector<int> idx(nb);
-            std::iota(idx.begin(), idx.end(), 0);
-            std::stable_sort(idx.begin(), idx.end(), [&](int a, int c){ return per_pass[k][a].tiles > per_pass[k][c].tiles; });
+        auto emit = [&](int k, int i){
+            BatchUnit U = per_pass[k][i];
+            U.dep = (k == 0) ? -1 : pos[(k - 1) * nb + i];
+            U.tile0 = total;
+            total += U.tiles;
+            pos[k * nb + i] = (int)units.size();
+            units.push_back(U);
+        };
+        // larger boxes first (balances the tail)
+        std::vector<int> idx(nb);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int c){ return per_pass[0][a].tiles > per_pass[0][c].tiles; });
+        if (config.group_mb <= 0){
+            // pass-major: pass 0 of every box, then pass 1, then pass 2
+            for (int k = 0; k < 3; k++)
+                for (int i : idx) emit(k, i);
+        } else {
+            // groups of boxes of about group_mb MB of spectrum each, in a
+            // three-step software pipeline: step s queues pass 2 of group s-2,
+            // pass 1 of group s-1 and pass 0 of group s, so a box's data is
+            // read again by its next pass about two groups' worth of work
+            // later, while it is still in L2 (every unit still comes after
+            // the unit it depends on)
+            std::vector<std::vector<int>> groups(1);
+            long long const cap = (long long)config.group_mb << 20;
+            long long acc = 0;
             for (int i : idx){
-                BatchUnit U = per_pass[k][i];
-                U.dep = (k == 0) ? -1 : pos[(k - 1) * nb + i];
-                U.tile0 = total;
-                total += U.tiles;
-                pos[k * nb + i] = (int)units.size();
-                units.push_back(U);
+                auto const &sz = sizes[i];
+                long long bytes = (long long)(r2c ? sz[0] / 2 + 1 : sz[0]) * sz[1] * sz[2] * (long long)csize;
+                if (!groups.back().empty() && acc + bytes > cap){ groups.emplace_back(); acc = 0; }
+                groups.back().push_back(i);
+                acc += bytes;
             }
+            int const ng = (int)groups.size();
+            for (int st = 0; st < ng + 2; st++)
+                for (int k = 2; k >= 0; k--){
+                    int g = st - k;
+                    if (g < 0 || g >= ng) continue;
+                    for (int i : groups[g]) emit(k, i);
+                }
         }
     };
     std::vector<BatchUnit> fu, bu;
@@ -437,6 +474,10 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     };
     for (auto const *v : {&fu, &bu}){
         bool fwd = (v == &fu);
+        // a unit waits only for units queued before it (no CTA can wait on a
+        // tile that no CTA has claimed yet)
+        for (size_t j = 0; j < v->size(); j++)
+            if ((*v)[j].dep >= (int)j) throw Error(ST_INVALID, "internal error: batch unit queued before its dependency");
         for (auto const &U : *v){
             long long N = b->ffts[U.plan]->N;
             // forward: input (in_total) -> output (out_total); backward: input
@@ -538,8 +579,9 @@ static void build_graph(Batch &b, bool fwd){
     (fwd ? b.fwd_knode : b.bwd_knode) = knode;
 }
 
-// Times forward + backward of every launch shape (prefetch on / off, tile
-// bounds of 48, 32 and 24 KB: 2 to 5 CTAs per SM) on the caller's buffers
+// Times forward + backward of every launch shape (queue order pass-major or
+// in groups of 16 or 32 MB, prefetch on / off, tile bounds of 48, 32 and 24
+// KB: 2 to 5 CTAs per SM) on the caller's buffers
 // and leaves `b` built with the fastest; the untuned default is a candidate,
 // so tuning never makes the batch slower than it was (within the timing noise).
 BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out, void *back, void *work, int reps,
@@ -555,11 +597,18 @@ BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out,
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
     check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
-    for (int pf : {1, 0}){
-        for (int kb : {48, 32, 24}){
-            BatchConfig c;
-            c.prefetch = pf;
-            c.tile_kb = kb;
+    std::vector<BatchConfig> shapes;
+    for (int gm : {0, 16, 32})
+        for (int pf : {0, 1})
+            for (int kb : {48, 32, 24}){
+                BatchConfig c;
+                c.prefetch = pf;
+                c.tile_kb = kb;
+                c.group_mb = gm;
+                shapes.push_back(c);
+            }
+    {
+        for (BatchConfig const &c : shapes){
             auto cand = make_batch(kind, prec, sizes, s, c);
             for (int i = 0; i < 2; i++){
                 cand->run(true, in, out, nullptr, 0);

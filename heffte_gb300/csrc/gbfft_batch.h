@@ -36,10 +36,14 @@ struct BatchBufs { void const *in; void *out; void *work; };
 // Launch shape of a batch: prefetch = 1 copies each CTA's next tile into
 // shared memory while it transforms the current one (when the next tile's
 // pass dependency is already met); tile_kb bounds the shared memory of one
-// tile's exchange buffer (smaller tiles: more CTAs per SM).
+// tile's exchange buffer (smaller tiles: more CTAs per SM); group_mb > 0
+// queues the boxes in groups of about that many MB of spectrum, each group's
+// passes two groups apart (its data stays in L2 between them), 0 queues
+// pass 0 of every box, then pass 1, then pass 2.
 struct BatchConfig {
-    int prefetch = 1;
+    int prefetch = 0;
     int tile_kb = 48;
+    int group_mb = 0;
 };
 struct BatchUnit;   // one 1-D pass of one box (gbfft_batch.cu)
 

@@ -80,10 +80,13 @@ __device__ __forceinline__ void fft_stage(Stage const &S, int t, int Tt, bool ac
     if (!to_global) __syncthreads();
 }
 
-// Called by every thread once the first stage has read all its inputs (the
-// default does nothing); the batch kernel starts the copy of its next tile
-// into the buffer the first stage read from.
-struct NoHook { __device__ __forceinline__ void operator()() const {} };
+// Called by every thread once the first stage has read all its inputs, when
+// enabled() (uniform over the CTA); the batch kernel starts the copy of its
+// next tile into the buffer the first stage read from.
+struct NoHook {
+    __device__ __forceinline__ bool enabled() const { return false; }
+    __device__ __forceinline__ void operator()() const {}
+};
 
 // Runs the whole transform. If last_to_global is false the result is left in
 // shared memory (natural order) and the CTA is synchronised on return.
@@ -100,7 +103,9 @@ __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t
             if (last_to_global) st(0, x); else sm[sm_index<COLS>(0, loc, TPB, padn)] = x;
         }
         if (!last_to_global) __syncthreads();
-        if constexpr (HOOK){ __syncthreads(); after_first(); }
+        if constexpr (HOOK){
+            if (after_first.enabled()){ __syncthreads(); after_first(); }
+        }
         return;
     }
     for (int s = 0; s < P.nstages; s++){
@@ -121,7 +126,7 @@ __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t
         if constexpr (HOOK){
             // a stage that ends in shared memory ends with a barrier; one that
             // stores to global memory needs one before the inputs are free
-            if (first){
+            if (first && after_first.enabled()){
                 if (tg) __syncthreads();
                 after_first();
             }

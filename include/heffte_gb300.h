@@ -333,20 +333,25 @@ int heffte_gb300_boxbatch_forward(heffte_gb300_boxbatch batch, const void *input
 int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *input, void *output, void *workspace,
                                    int scale);
 
-/* No reference counterpart.  Launch shape of a batch: prefetch = 1 (default)
- * copies each CTA's next tile into shared memory while the CTA transforms
- * the current one (when that tile's pass dependency is already met);
+/* No reference counterpart.  Launch shape of a batch: prefetch = 1 copies
+ * each CTA's next tile into shared memory while the CTA transforms the
+ * current one (when that tile's pass dependency is already met; default 0);
  * tile_kb (8..96, default 48) bounds one tile's shared exchange buffer, so
- * smaller values give smaller tiles and more CTAs per SM.  Results are the
- * same for every shape.  configure() rebuilds the batch with a shape;
- * autotune() times forward (input -> output) + backward (output -> back,
- * with workspace) `reps` times for every shape (prefetch on / off, 48, 32, 24
- * KB), keeps the fastest, and returns it with its ms per forward + backward;
- * it overwrites output, back and workspace, and leaves input as it was. */
-int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch batch, int prefetch, int tile_kb);
-int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch batch, int *prefetch, int *tile_kb);
+ * smaller values give smaller tiles and more CTAs per SM; group_mb (0..4096,
+ * default 0) > 0 queues the boxes in groups of about that many MB of
+ * spectrum with each group's passes two groups apart, so a box's data stays
+ * in L2 from one pass to the next (0: pass 0 of every box, then pass 1, then
+ * pass 2).  Results are the same for every shape.  configure() rebuilds the
+ * batch with a shape; autotune() times forward (input -> output) + backward
+ * (output -> back, with workspace) `reps` times for every shape (groups of
+ * 0, 16, 32 MB x prefetch on / off x 48, 32, 24 KB), keeps the fastest, and
+ * returns it with its ms per forward + backward; it overwrites output, back
+ * and workspace, and leaves input as it was. */
+int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch batch, int prefetch, int tile_kb, int group_mb);
+int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch batch, int *prefetch, int *tile_kb, int *group_mb);
 int heffte_gb300_boxbatch_autotune(heffte_gb300_boxbatch batch, const void *input, void *output, void *back,
-                                   void *workspace, int reps, int *prefetch, int *tile_kb, double *ms);
+                                   void *workspace, int reps, int *prefetch, int *tile_kb, int *group_mb,
+                                   double *ms);
 
 /* No reference counterpart.  Clock budget (GPU clocks, >= 0) after which the
  * batch kernel's wait for another CTA's pass of the same box gives up, records
