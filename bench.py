@@ -508,6 +508,8 @@ WORKLOADS = {
     "batch256prefetch": ("batch", "prefetch", 0),
     # the same queued in groups of 16 MB of boxes, each group's passes two groups apart (L2-resident)
     "batch256grouped": ("batch", "grouped", 0),
+    # the same with 16 values per thread (radix-16 plans; the default holds 8)
+    "batch256values16": ("batch", "values16", 0),
     # the same boxes as a loop over one fft3d_r2c plan per box (how the reference runs them)
     "batch256loop": ("batch", "loop", 0),
     # learned plan selection on the 2000 measured shapes (tests/golden/selector_timings.npz)
@@ -584,7 +586,7 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     if tune_cache == "loop":
         return run_batch_loop(name, sizes, steps, warmup)
     # launch shapes other than the default (prefetch, tile KB, group MB)
-    fixed = {"prefetch": (1, 48, 0), "grouped": (0, 48, 16)}.get(tune_cache)
+    fixed = {"prefetch": (1, 48, 0, 0), "grouped": (0, 48, 16, 0), "values16": (0, 48, 0, 16)}.get(tune_cache)
     if fixed:
         tune_cache = None
     plans = None
@@ -607,8 +609,8 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     shape = None
     if tune_cache is not None:
         # the launch shape (prefetch, tile bound, queue groups) timed on these buffers
-        pf, kb, gm, tms = b.autotune(x, y, z, w, reps=5)
-        shape = {"prefetch": pf, "tile_kb": kb, "group_mb": gm, "ms_at_tuning": tms}
+        pf, kb, gm, vals, tms = b.autotune(x, y, z, w, reps=5)
+        shape = {"prefetch": pf, "tile_kb": kb, "group_mb": gm, "values": vals, "ms_at_tuning": tms}
 
     def step():
         b.forward(x, y, gb.scale.full)
@@ -631,7 +633,7 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     return {"workload": name, "boxes": len(sizes), "ms_per_step": ms, "gflops": flops / (ms / 1e3) / 1e9,
             "gbs": byts / (ms / 1e3) / 1e9, "hbm_frac": byts / (ms / 1e3) / 1e9 / peak,
             "roundtrip_max_abs": err, "launches_per_step": 2, "tuned": tune_cache is not None,
-            "launch_shape": dict(zip(("prefetch", "tile_kb", "group_mb"), b.config())),
+            "launch_shape": dict(zip(("prefetch", "tile_kb", "group_mb", "values"), b.config())),
             **({"tuned_plans": plans} if plans else {}), **({"tuned_shape": shape} if shape else {})}
 
 
@@ -851,7 +853,7 @@ def run_workload(name, steps, warmup):
         out["double_arithmetic"] = arith
         return out
     if kind == "batch":
-        cache = size if size in ("loop", "prefetch", "grouped") else None
+        cache = size if size in ("loop", "prefetch", "grouped", "values16") else None
         if size == "tuned":
             import tempfile
             cache = os.path.join(tempfile.mkdtemp(), "tune.tsv")

@@ -104,12 +104,10 @@ def lib():
     L.heffte_gb300_set_dependency_wait_budget.argtypes = [ll]
     L.heffte_gb300_dependency_wait_budget.restype = ll
     L.heffte_gb300_boxbatch_hold_dependencies.argtypes = [vp, i]
-    L.heffte_gb300_boxbatch_configure.argtypes = [vp, i, i, i]
-    L.heffte_gb300_boxbatch_config.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
-                                               ctypes.POINTER(ctypes.c_int)]
-    L.heffte_gb300_boxbatch_autotune.argtypes = [vp, vp, vp, vp, vp, i, ctypes.POINTER(ctypes.c_int),
-                                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
-                                                 ctypes.POINTER(ctypes.c_double)]
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.heffte_gb300_boxbatch_configure.argtypes = [vp, i, i, i, i]
+    L.heffte_gb300_boxbatch_config.argtypes = [vp, ip, ip, ip, ip]
+    L.heffte_gb300_boxbatch_autotune.argtypes = [vp, vp, vp, vp, vp, i, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_double)]
     L.heffte_gb300_boxbatch_forward.argtypes = [vp, vp, vp, i]
     L.heffte_gb300_boxbatch_backward.argtypes = [vp, vp, vp, vp, i]
     L.heffte_gb300_tune.argtypes = [i, i, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_int)]
@@ -544,25 +542,27 @@ class boxbatch:
     def workspace_size(self):
         return lib().heffte_gb300_boxbatch_workspace_size(self._h)
 
-    def configure(self, prefetch=0, tile_kb=48, group_mb=0):
+    def configure(self, prefetch=0, tile_kb=48, group_mb=0, values=0):
         """Launch shape: prefetch of each CTA's next tile, tile bound in KB,
-        queue order (boxes in L2-sized groups of group_mb MB, 0: pass-major)."""
-        check(lib().heffte_gb300_boxbatch_configure(self._h, int(prefetch), int(tile_kb), int(group_mb)))
+        queue order (boxes in L2-sized groups of group_mb MB, 0: pass-major),
+        complex values per thread (8, 16, 0: 8 where the sides allow it)."""
+        check(lib().heffte_gb300_boxbatch_configure(self._h, int(prefetch), int(tile_kb), int(group_mb), int(values)))
 
     def config(self):
-        pf, kb, gm = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
-        check(lib().heffte_gb300_boxbatch_config(self._h, ctypes.byref(pf), ctypes.byref(kb), ctypes.byref(gm)))
-        return pf.value, kb.value, gm.value
+        """(prefetch, tile_kb, group_mb, values per thread in use)."""
+        v = [ctypes.c_int(0) for _ in range(4)]
+        check(lib().heffte_gb300_boxbatch_config(self._h, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
 
     def autotune(self, inarray, outarray, back, workspace, reps=5):
         """Times every launch shape on these buffers (forward in -> out,
         backward out -> back) and keeps the fastest; returns (prefetch,
-        tile_kb, group_mb, ms per forward + backward)."""
-        pf, kb, gm, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        tile_kb, group_mb, values, ms per forward + backward)."""
+        v = [ctypes.c_int(0) for _ in range(4)]
+        ms = ctypes.c_double(0)
         check(lib().heffte_gb300_boxbatch_autotune(self._h, _ptr(inarray), _ptr(outarray), _ptr(back), _ptr(workspace),
-                                                   int(reps), ctypes.byref(pf), ctypes.byref(kb), ctypes.byref(gm),
-                                                   ctypes.byref(ms)))
-        return pf.value, kb.value, gm.value, ms.value
+                                                   int(reps), *[ctypes.byref(x) for x in v], ctypes.byref(ms)))
+        return tuple(x.value for x in v) + (ms.value,)
 
     def hold_dependencies(self, hold):
         """Test hook: every pass dependency waits for a tile that never comes

@@ -13,260 +13,12 @@
 // functions use __ldcg).  Radix plans and tile sizes per transform length come
 // from the autotuner when it has measured them (gbfft_tune.cu).
 #include "gbfft_batch.h"
-#include "gbfft_kernels.cuh"
-#include "gbfft_ptx.cuh"
+#include "gbfft_batch_kernel.cuh"
+#include <algorithm>
 #include <atomic>
 #include <numeric>
 
 namespace gbfft {
-
-struct BatchUnit {
-    int kind;            // K_R2C, K_C2R, K_C2C_F, K_C2C_B
-    int cols;            // column layout (1) or lines (0)
-    int plan;            // index into the plan table
-    int tpb;             // transforms (or pairs) per tile
-    int src, dst;        // buffers: 0 input, 1 output, 2 workspace
-    int dep;             // unit that must complete first (-1: none)
-    int dep_extra;       // tiles awaited beyond the dependency's own (0; 1 only under hold_dependencies)
-    int last;            // carries the scale
-    long long G;         // transforms of this pass
-    long long tiles, tile0;
-    long long in_off, out_off;   // element offsets into the source / destination buffer
-    Layout Li, Lo;
-    double scale;
-    int pf;              // the input of a tile can be copied ahead into shared memory (lines back to back, or adjacent columns)
-};
-
-// Copy of a tile's input into shared memory: `rows` rows of `rowbytes`
-// contiguous bytes, srcstride apart in global memory and dststride apart in
-// shared memory (every figure a multiple of 16 bytes).
-struct TileCopy {
-    unsigned char const *src;
-    long long srcstride;
-    int rows, rowbytes, dststride;
-};
-
-// The copy plan of tile lt of unit U, or false when the tile does not meet
-// the 16-byte granularity of the asynchronous copy (or spans two blocks).
-// Shared-memory layout: lines back to back (what tile_r2c / tile_c2r /
-// tile_c2c read for line tiles), or one row of TPB columns per element
-// position (column tiles).
-template<typename T>
-__device__ __forceinline__ bool tile_copy_plan(BatchUnit const &U, Plan1D const &P, BatchBufs const &bufs, long long lt,
-                                               TileCopy &tc){
-    using C = c_t<T>;
-    if (!U.pf) return false;
-    unsigned char const *srcb = reinterpret_cast<unsigned char const*>(U.src == 0 ? bufs.in : (U.src == 1 ? bufs.out : bufs.work));
-    int const N = P.N;
-    if (!U.cols){
-        int const per = (U.kind == K_R2C || U.kind == K_C2R) ? 2 : 1;
-        int const len = (U.kind == K_C2R) ? N / 2 + 1 : N;
-        long long const es = (U.kind == K_R2C) ? (long long)sizeof(T) : (long long)sizeof(C);
-        long long const first = lt * (long long)U.tpb * per;
-        long long const lines = min((long long)U.tpb * per, U.G - first);
-        unsigned char const *src = srcb + (U.in_off + first * len) * es;
-        long long const bytes = lines * len * es;
-        if ((reinterpret_cast<uintptr_t>(src) & 15) || (bytes & 15)) return false;
-        tc.src = src; tc.srcstride = 0; tc.rows = 1; tc.rowbytes = (int)bytes; tc.dststride = 0;
-        return true;
-    }
-    long long const es = sizeof(C);
-    long long const g0 = lt * (long long)U.tpb;
-    long long const W = min((long long)U.tpb, U.G - g0);
-    long long const blk = g0 / U.Li.count, c0 = g0 - blk * U.Li.count;
-    if (c0 + W > U.Li.count) return false;
-    unsigned char const *src = srcb + (U.in_off + blk * U.Li.bstride + c0) * es;
-    // both sides of every 16-byte copy aligned: the source start and row
-    // stride, the row length, and the shared-memory row stride (TPB columns)
-    if ((reinterpret_cast<uintptr_t>(src) & 15) || ((W * es) & 15) || ((U.Li.estride * es) & 15) ||
-        (((long long)U.tpb * es) & 15))
-        return false;
-    tc.src = src; tc.srcstride = U.Li.estride * es; tc.rows = N; tc.rowbytes = (int)(W * es);
-    tc.dststride = (int)(U.tpb * es);
-    return true;
-}
-
-// 16-byte asynchronous copy global -> shared through L2 only (.cg): the
-// data was written by other CTAs of the same launch, so this SM's L1 may
-// hold stale lines of it
-__device__ __forceinline__ void cp_async_cg16(void *dst, void const *src){
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(smem_u32(dst)), "l"(src) : "memory");
-}
-
-// CTAs per SM the batch kernels are compiled for (registers per thread
-// <= 65536 / (256 x this)); float measured best at 4, double kept at 2
-template<typename T> constexpr int batch_ctas_per_sm(){ return sizeof(T) == 4 ? 4 : 2; }
-
-// scaling: 0 none, 1 full (1/N of each box), 2 symmetric.  One kernel per
-// direction: the forward one holds the r2c and forward c2c tile paths, the
-// backward one the backward c2c and c2r paths (fewer paths, fewer
-// registers), compiled for several CTAs per SM: the stage-0 loads of small
-// tiles are latency-bound, and more warps per SM hide them better than the
-// few spills cost (256 uneven r2c float boxes, ms per step: 2.09 at one CTA
-// per SM, 1.54 at two, 1.46 at three, 1.38 at four, 1.64-1.80 at five to
-// eight).
-// the stage-0 hook of the batch kernel: on only when the batch prefetches
-template<class F> struct PrefetchHook {
-    F const &f;
-    bool on;
-    __device__ __forceinline__ bool enabled() const { return on; }
-    __device__ __forceinline__ void operator()() const { f(); }
-};
-
-template<typename T, bool FWD>
-__global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
-k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
-        c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
-        long long total_tiles, int *status, int scaling, long long dep_budget, int pf_offset){
-    using C = c_t<T>;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    C *sm = reinterpret_cast<C*>(smraw);
-    // prefetch buffer after the exchange buffer (pf_offset < 0: no prefetch)
-    unsigned char *pfbuf = smraw + (pf_offset > 0 ? pf_offset : 0);
-    __shared__ long long s_tile, s_next;
-    __shared__ int s_unit, s_next_unit, s_pf_cur, s_pf_next;
-    __shared__ TileCopy s_copy;
-    // first tile of every unit, for the tile -> unit search (shared memory
-    // when it fits, else the unit table itself)
-    constexpr int kUnitsInSmem = 1024;
-    __shared__ long long s_tile0[kUnitsInSmem];
-    int tid = threadIdx.x;
-    bool const smem_units = nunits <= kUnitsInSmem;
-    if (smem_units)
-        for (int i = tid; i < nunits; i += blockDim.x) s_tile0[i] = units[i].tile0;
-    __syncthreads();
-    auto find_unit = [&](long long t) -> int {      // last unit with tile0 <= t
-        int lo = 0, hi = nunits - 1;
-        while (lo < hi){
-            int mid = (lo + hi + 1) >> 1;
-            long long t0 = smem_units ? s_tile0[mid] : units[mid].tile0;
-            if (t0 <= t) lo = mid; else hi = mid - 1;
-        }
-        return lo;
-    };
-    // the next tile is claimed (and its unit found) while the current one is
-    // processed, so the queue atomic's latency is hidden; the smallest
-    // unfinished tile is always some CTA's current tile and depends only on
-    // smaller ones, so claiming ahead cannot stall the queue
-    if (tid == 0){
-        s_next = (long long)atomicAdd(work_counter, 1ull);
-        s_next_unit = (s_next < total_tiles) ? find_unit(s_next) : 0;
-        s_pf_next = 0;
-    }
-    __syncthreads();
-    while (true){
-        if (tid == 0){
-            s_tile = s_next;
-            s_unit = s_next_unit;
-            s_pf_cur = s_pf_next;
-            s_pf_next = 0;
-            if (s_tile < total_tiles){
-                long long nx = (long long)atomicAdd(work_counter, 1ull);
-                s_next = nx;
-                s_next_unit = (nx < total_tiles) ? find_unit(nx) : 0;
-            }
-        }
-        __syncthreads();
-        long long gt = s_tile;
-        int u = s_unit;
-        bool const pfcur = s_pf_cur != 0;
-        if (gt >= total_tiles) return;
-        BatchUnit const &U = units[u];
-        bool ok = true;
-        // a prefetched tile's dependency was met before its copy was issued
-        if (tid == 0 && U.dep >= 0 && !pfcur){
-            long long need = units[U.dep].tiles + U.dep_extra;
-            volatile int *d = done + U.dep;
-            if (*d < need){
-                long long t0 = clock64();
-                while (*d < need){
-                    if (clock64() - t0 > dep_budget){ atomicExch(status, DEV_TIMEOUT_DEPENDENCY); ok = false; break; }
-                }
-            }
-            __threadfence();
-        }
-        if (__syncthreads_or(!ok)) return;
-        if (pfcur){
-            asm volatile("cp.async.wait_all;" ::: "memory");
-            __syncthreads();
-        }
-        // once stage 0 has read this tile's inputs, the claimed next tile's
-        // input goes into the prefetch buffer if its dependency is met
-        auto prefetch_next = [&](){
-            if (tid == 0){
-                int go = 0;
-                if (pf_offset > 0 && s_next < total_tiles){
-                    BatchUnit const &V = units[s_next_unit];
-                    bool met = true;
-                    if (V.dep >= 0){
-                        volatile int *d = done + V.dep;
-                        met = *d >= units[V.dep].tiles + V.dep_extra;
-                    }
-                    TileCopy tc;
-                    if (met && tile_copy_plan<T>(V, plans[V.plan], bufs, s_next - V.tile0, tc)){
-                        __threadfence();
-                        s_copy = tc;
-                        go = 1;
-                    }
-                }
-                s_pf_next = go;
-            }
-            __syncthreads();
-            if (s_pf_next){
-                TileCopy const tc = s_copy;
-                int const cpr = tc.rowbytes >> 4;
-                long long const total = (long long)tc.rows * cpr;
-                for (long long c = tid; c < total; c += blockDim.x){
-                    int const r = (int)(c / cpr), k = (int)(c - (long long)r * cpr);
-                    cp_async_cg16(pfbuf + (long long)r * tc.dststride + 16 * k, tc.src + r * tc.srcstride + 16 * k);
-                }
-                asm volatile("cp.async.commit_group;" ::: "memory");
-            }
-        };
-        PrefetchHook<decltype(prefetch_next)> const hook{prefetch_next, pf_offset > 0};
-        long long lt = gt - U.tile0;
-        Plan1D const &P = plans[U.plan];
-        C const *tw = tws[U.plan];
-        unsigned char const *srcb = reinterpret_cast<unsigned char const*>(U.src == 0 ? bufs.in : (U.src == 1 ? bufs.out : bufs.work));
-        unsigned char *dstb = reinterpret_cast<unsigned char*>(U.dst == 1 ? bufs.out : bufs.work);
-        double f = (scaling == 0) ? 1.0 : ((scaling == 1) ? U.scale : sqrt(U.scale));
-        T sc = (T)f;
-        int dsc = U.last && scaling != 0;
-        C const *pfc = pfcur ? reinterpret_cast<C const*>(pfbuf) : nullptr;
-        if constexpr (FWD){
-            if (U.kind == K_R2C){
-                T const *in = reinterpret_cast<T const*>(srcb) + U.in_off;
-                C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                T const *pfr = pfcur ? reinterpret_cast<T const*>(pfbuf) : nullptr;
-                if (U.cols) tile_r2c<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
-                else tile_r2c<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
-            } else {
-                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
-                C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, kEmax, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else tile_c2c<T, kEmax, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-            }
-        } else {
-            if (U.kind == K_C2R){
-                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
-                T *out = reinterpret_cast<T*>(dstb) + U.out_off;
-                if (U.cols) tile_c2r<T, kEmax, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else tile_c2r<T, kEmax, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-            } else {
-                C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
-                C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, kEmax, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else tile_c2c<T, kEmax, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-            }
-        }
-        // publish completion of this tile
-        __syncthreads();
-        if (tid == 0){
-            __threadfence();
-            atomicAdd(done + u, 1);
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -300,21 +52,49 @@ Batch::~Batch(){
     for (void *p : device_allocs) cudaFree(p);
 }
 
-static void const *batch_kernel(int prec, bool fwd){
-    if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true>)
-                              : reinterpret_cast<void const*>(k_batch<float, false>);
-    return fwd ? reinterpret_cast<void const*>(k_batch<double, true>)
-               : reinterpret_cast<void const*>(k_batch<double, false>);
+static void const *batch_kernel(int prec, bool fwd, int values){
+    return values == 8 ? batch_kernel_e8(prec, fwd) : batch_kernel_e16(prec, fwd);
 }
 
-static int tile_tpb(Fft1D const &f, bool cols, bool paired, size_t csize, size_t smem_cap, int tune_tpb){
-    int T = f.plan.T;
+static int tile_tpb(Plan1D const &P, bool cols, size_t csize, size_t smem_cap, int tune_tpb){
+    int const T = P.T, N = P.N;
     int tpb = (tune_tpb > 0) ? tune_tpb : std::max(1, kBatchThreads / T);
     tpb = std::min(tpb, std::max(1, kBatchThreads / T));
-    size_t unit = cols ? (size_t)f.N * csize : (size_t)(f.N + (f.N >> 4) + 1) * csize;
+    size_t unit = cols ? (size_t)N * csize : (size_t)(N + (N >> 4) + 1) * csize;
     while (tpb > 1 && tpb * unit > smem_cap) tpb--;
-    (void)paired;
     return tpb;
+}
+
+// Radix plan of N with radices up to 8 (the 8-values-per-thread kernel):
+// radix-8 stages, the remaining power of two as 4 or 4 x 4 (never a radix 2
+// beside an 8), then the odd primes; empty when N has a prime factor above 7.
+static std::vector<int> radices_upto8(int N){
+    std::vector<int> odd;
+    int n = N;
+    for (int p : {7, 5, 3})
+        while (n % p == 0){ odd.push_back(p); n /= p; }
+    int a = 0;
+    while (n % 2 == 0){ n /= 2; a++; }
+    if (n != 1) return {};
+    std::vector<int> r;
+    int q = a / 3, rem = a % 3;
+    if (rem == 1 && q >= 1){ q -= 1; r = {4, 4}; }
+    else if (rem == 1) r = {2};
+    else if (rem == 2) r = {4};
+    for (int i = 0; i < q; i++) r.insert(r.begin(), 8);
+    r.insert(r.end(), odd.begin(), odd.end());
+    return r;
+}
+
+// Threads per transform when each thread holds `values` values: a stage of
+// radix R gives each thread values / R butterflies.
+static int threads_per_transform(Plan1D const &P, int values){
+    int T = 1;
+    for (int s = 0; s < P.nstages; s++){
+        int per = values / P.st[s].R;
+        T = std::max(T, (P.st[s].NR + per - 1) / per);
+    }
+    return T;
 }
 
 std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int, 3>> const &sizes, cudaStream_t stream,
@@ -325,6 +105,8 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     if (config.prefetch != 0 && config.prefetch != 1) throw Error(ST_INVALID, "prefetch must be 0 or 1");
     if (config.tile_kb < 8 || config.tile_kb > 96) throw Error(ST_INVALID, "tile size must be 8 to 96 KB");
     if (config.group_mb < 0 || config.group_mb > 4096) throw Error(ST_INVALID, "group size must be 0 to 4096 MB");
+    if (config.values != 0 && config.values != 8 && config.values != 16)
+        throw Error(ST_INVALID, "values per thread must be 0 (automatic), 8 or 16");
     auto b = std::make_unique<Batch>();
     b->kind = kind; b->prec = prec; b->sizes = sizes; b->stream = stream;
     b->config = config;
@@ -352,18 +134,37 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     for (auto const &s : sizes) for (int d = 0; d < 3; d++) lens.push_back(s[d]);
     std::sort(lens.begin(), lens.end());
     lens.erase(std::unique(lens.begin(), lens.end()), lens.end());
+    // 8 values per thread when every length has a plan of radices up to 8
+    // (automatic: then; 16 takes any plan)
+    bool const fits8 = std::all_of(lens.begin(), lens.end(), [](int N){ return N == 1 || !radices_upto8(N).empty(); });
+    if (config.values == 8 && !fits8)
+        throw Error(ST_UNSUPPORTED, "8 values per thread need box sides with prime factors up to 7");
+    int const values = (config.values == 0) ? (fits8 ? 8 : 16) : config.values;
+    b->values = values;
     std::map<int, int> plan_of;
     std::vector<Plan1D> plans;
     std::vector<void const*> tws;
     std::vector<int> tpb_hint;
     for (int N : lens){
         TuneChoice tc = tuned_choice(N, prec);
-        auto f = get_fft1d(N, tc.radices);
+        std::vector<int> rad = tc.radices;
+        int hint = tc.tpb;
+        if (values == 8){
+            // a tuned plan only if its radices fit (it was then timed at 8 values)
+            bool ok = !rad.empty() && std::all_of(rad.begin(), rad.end(), [](int r){ return r <= 8; });
+            if (!ok){
+                rad = (N == 1) ? std::vector<int>{} : radices_upto8(N);
+                hint = 0;
+            }
+        }
+        auto f = get_fft1d(N, rad);
+        Plan1D P = f->plan;
+        P.T = threads_per_transform(P, values);
         plan_of[N] = (int)plans.size();
-        plans.push_back(f->plan);
+        plans.push_back(P);
         tws.push_back(f->twiddles(prec, stream));
         b->ffts.push_back(f);
-        tpb_hint.push_back(tc.tpb);
+        tpb_hint.push_back(hint);
     }
     size_t smem_cap = (size_t)config.tile_kb * 1024;
     // units: forward = (r2c|c2c x), c2c y, c2c z; backward = c2c z, c2c y, (c2r|c2c x)
@@ -390,7 +191,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
                 U.plan = plan_of[(int)rbox.size[d]];
                 Fft1D const &f = *b->ffts[U.plan];
                 bool paired = is_r2x;
-                U.tpb = tile_tpb(f, U.cols, paired, csize, smem_cap, tpb_hint[U.plan]);
+                U.tpb = tile_tpb(plans[U.plan], U.cols, csize, smem_cap, tpb_hint[U.plan]);
                 long long units_n = paired ? (U.G + 1) / 2 : U.G;
                 U.tiles = (units_n + U.tpb - 1) / U.tpb;
                 // buffers: forward input -> output (in place after the first pass);
@@ -533,7 +334,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     if (b->pf_offset > 0) smem += (pf_bytes + 15) / 16 * 16;
     b->smem = smem;
     for (bool fwd : {true, false}){
-        void const *kern = batch_kernel(prec, fwd);
+        void const *kern = batch_kernel(prec, fwd, values);
         int nb_sm = 1;
         check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
         check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, kern, kBatchThreads, smem), "occupancy");
@@ -569,7 +370,7 @@ static void build_graph(Batch &b, bool fwd){
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
                     &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget, &b.pf_offset};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd));
+    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values));
     kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)b.smem;
@@ -579,9 +380,9 @@ static void build_graph(Batch &b, bool fwd){
     (fwd ? b.fwd_knode : b.bwd_knode) = knode;
 }
 
-// Times forward + backward of every launch shape (queue order pass-major or
-// in groups of 16 or 32 MB, prefetch on / off, tile bounds of 48, 32 and 24
-// KB: 2 to 5 CTAs per SM) on the caller's buffers
+// Times forward + backward of every launch shape (16 or 8 values per thread,
+// queue order pass-major or in groups of 16 MB, prefetch on / off, tile
+// bounds of 48, 32 and 24 KB: 2 to 5 CTAs per SM) on the caller's buffers
 // and leaves `b` built with the fastest; the untuned default is a candidate,
 // so tuning never makes the batch slower than it was (within the timing noise).
 BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out, void *back, void *work, int reps,
@@ -598,18 +399,26 @@ BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out,
     check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
     check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
     std::vector<BatchConfig> shapes;
-    for (int gm : {0, 16, 32})
-        for (int pf : {0, 1})
-            for (int kb : {48, 32, 24}){
-                BatchConfig c;
-                c.prefetch = pf;
-                c.tile_kb = kb;
-                c.group_mb = gm;
-                shapes.push_back(c);
-            }
+    for (int vals : {16, 8})
+        for (int gm : {0, 16})
+            for (int pf : {0, 1})
+                for (int kb : {48, 32, 24}){
+                    BatchConfig c;
+                    c.prefetch = pf;
+                    c.tile_kb = kb;
+                    c.group_mb = gm;
+                    c.values = vals;
+                    shapes.push_back(c);
+                }
     {
         for (BatchConfig const &c : shapes){
-            auto cand = make_batch(kind, prec, sizes, s, c);
+            std::unique_ptr<Batch> cand;
+            try {
+                cand = make_batch(kind, prec, sizes, s, c);
+            } catch (Error const &e){
+                if (e.code == ST_UNSUPPORTED && c.values == 8) continue;     // sides with factors above 7
+                throw;
+            }
             for (int i = 0; i < 2; i++){
                 cand->run(true, in, out, nullptr, 0);
                 cand->run(false, out, back, work, 0);
@@ -655,7 +464,7 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
                     &args_total, &args_status, &args_scaling, &args_budget, &pf_offset};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(prec, fwd));
+    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values));
     kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)smem;

@@ -39,11 +39,14 @@ struct BatchBufs { void const *in; void *out; void *work; };
 // tile's exchange buffer (smaller tiles: more CTAs per SM); group_mb > 0
 // queues the boxes in groups of about that many MB of spectrum, each group's
 // passes two groups apart (its data stays in L2 between them), 0 queues
-// pass 0 of every box, then pass 1, then pass 2.
+// pass 0 of every box, then pass 1, then pass 2; values: complex values each
+// thread holds (8: radix plans up to 8, fewer registers, box sides with prime
+// factors up to 7; 16: any plan; 0: 8 where the sides allow it).
 struct BatchConfig {
     int prefetch = 0;
     int tile_kb = 48;
     int group_mb = 0;
+    int values = 0;
 };
 struct BatchUnit;   // one 1-D pass of one box (gbfft_batch.cu)
 
@@ -62,6 +65,7 @@ struct Batch {
     size_t smem = 0;
     BatchConfig config;
     int pf_offset = -1;    // byte offset of the prefetch buffer in dynamic shared memory (-1: none)
+    int values = 16;       // complex values per thread of the kernel in use (8 or 16)
     int grid = 0;          // persistent CTAs of the forward kernel
     int grid_bwd = 0;      // and of the backward kernel
     cudaGraph_t fwd_graph = nullptr, bwd_graph = nullptr;

@@ -423,7 +423,7 @@ int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch b, const void *input, v
     });
 }
 
-int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch b, int prefetch, int tile_kb, int group_mb){
+int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch b, int prefetch, int tile_kb, int group_mb, int values){
     return guard([&]{
         if (!b) throw Error(ST_INVALID, "null batch");
         Batch const &B = *b->b;
@@ -431,27 +431,31 @@ int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch b, int prefetch, int t
         c.prefetch = prefetch;
         c.tile_kb = tile_kb;
         c.group_mb = group_mb;
+        c.values = values;
         b->b = make_batch(B.kind, B.prec, B.sizes, B.stream, c);
     });
 }
 
-int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch b, int *prefetch, int *tile_kb, int *group_mb){
+int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch b, int *prefetch, int *tile_kb, int *group_mb, int *values){
     return guard([&]{
-        if (!b || !prefetch || !tile_kb || !group_mb) throw Error(ST_INVALID, "null pointer");
+        if (!b || !prefetch || !tile_kb || !group_mb || !values) throw Error(ST_INVALID, "null pointer");
         *prefetch = b->b->config.prefetch;
         *tile_kb = b->b->config.tile_kb;
         *group_mb = b->b->config.group_mb;
+        *values = b->b->values;
     });
 }
 
 int heffte_gb300_boxbatch_autotune(heffte_gb300_boxbatch b, const void *input, void *output, void *back,
-                                   void *workspace, int reps, int *prefetch, int *tile_kb, int *group_mb, double *ms){
+                                   void *workspace, int reps, int *prefetch, int *tile_kb, int *group_mb,
+                                   int *values, double *ms){
     return guard([&]{
         if (!b) throw Error(ST_INVALID, "null batch");
         BatchConfig c = autotune_batch(b->b, input, output, back, workspace, reps, ms);
         if (prefetch) *prefetch = c.prefetch;
         if (tile_kb) *tile_kb = c.tile_kb;
         if (group_mb) *group_mb = c.group_mb;
+        if (values) *values = b->b->values;
     });
 }
 

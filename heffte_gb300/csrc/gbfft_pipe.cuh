@@ -70,13 +70,15 @@ __host__ __device__ constexpr int pipe_padn(int N){ return N + N / 16 + 1; }
 __host__ __device__ constexpr bool pipe_paired(int kind){ return kind >= PK_R2C_FWD; }
 // units (complex transforms or real pairs) per tile.  df: the double-float
 // complex<double> kernels, which are bound by the latency of their FP32
-// dependency chains rather than by memory: CTAs of about 128 threads and two
-// tile slots (at most ~100 KB of shared memory) so that two or three CTAs
-// share an SM and more warps hide that latency.
+// dependency chains rather than by memory: CTAs of about 128 threads with
+// one tile slot and no separate exchange buffer (line tiles exchange in the
+// tile buffer, swizzled), so that four or five CTAs share an SM and their
+// warps hide that latency (one slot: 21.7 against 29.0 ms with two slots for
+// a 512^3 complex<double> forward + backward).
 __host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols, bool df = false){
     if (df){
         int tpb = (128 / pipe_tt(N) > 1) ? 128 / pipe_tt(N) : 1;
-        while (tpb > 1 && 2 * (N + 4) * tpb * csize + (cols ? 0 : tpb * pipe_padn(N) * csize) > 100 * 1024) tpb /= 2;
+        while (tpb > 1 && (N + 4) * tpb * csize > 64 * 1024) tpb /= 2;
         return tpb;
     }
     int tt = pipe_tt(N);
@@ -103,7 +105,11 @@ __host__ __device__ constexpr int pipe_tile_elems(int N, int tpb, int kind){
 // column tiles of the tensor-map loader whose two buffers already take more
 // than half of an SM's shared memory (one CTA per SM, so a deeper prefetch is
 // what keeps more copies in flight), two otherwise.
+#ifndef GBFFT_DF_SLOTS
+#define GBFFT_DF_SLOTS 1
+#endif
 __host__ __device__ constexpr int pipe_nbuf(int N, int csize, bool cols, int kind, int loader, bool df = false){
+    if (df && loader != LD_CPASYNC) return GBFFT_DF_SLOTS;
     return (!df && cols && loader == LD_TENSOR && (kind == PK_C2C_FWD || kind == PK_C2C_BWD) &&
             2 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize > 114 * 1024 &&
             3 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize <= 200 * 1024) ? 3 : 2;
@@ -111,7 +117,7 @@ __host__ __device__ constexpr int pipe_nbuf(int N, int csize, bool cols, int kin
 __host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind, int loader, bool df = false){
     int tpb = pipe_tpb(N, csize, cols, df);
     return pipe_nbuf(N, csize, cols, kind, loader, df) * pipe_tile_elems(N, tpb, kind) * csize +
-           (cols ? 0 : tpb * pipe_padn(N) * csize);
+           ((cols || df) ? 0 : tpb * pipe_padn(N) * csize);
 }
 
 struct PipeParams {
@@ -133,12 +139,22 @@ struct PipeParams {
     int *status;
 };
 
+// Position of element p within a line of the swizzled exchange: the low three
+// bits XORed with the three-bit groups above them, so that the eight 16-byte
+// accesses of a quarter warp at any power-of-two stride (1 .. 256 elements)
+// fall on distinct bank groups; a permutation within each aligned 8 elements.
+__host__ __device__ constexpr int pipe_swz(int p){
+    return p ^ (((p >> 3) ^ (p >> 6) ^ (p >> 9)) & 7);
+}
+
 // One radix stage; S == 0 reads through ld0, the last stage writes through st
 // (or to the exchange buffer when POST is set).  Stages S .. SEND-1 run
 // (SEND below the stage count stops early, the last run stage writing the
 // exchange buffer).
-template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST, int SEND = pipe_nstages(N), class LD,
-         class ST>
+// SWZ: line tiles exchanged in the tile buffer itself (pitch N), element p of
+// a line at pipe_swz(p) (no padding, the bank spread of an XOR swizzle).
+template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST, int SEND = pipe_nstages(N),
+         bool SWZ = false, class LD, class ST>
 __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const *__restrict__ tw,
                                        c_t<T> (&v)[16], LD &ld0, ST &st){
     using C = c_t<T>;
@@ -149,7 +165,11 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
         constexpr bool LAST = (S == NS - 1);
         constexpr bool TO_XCH = !LAST || POST;
         constexpr int LNS = cilog2(Ns), LNSR = cilog2(Ns * R);
-        auto xi = [&](int p) -> int { return COLS ? (p * TPB + loc) : (loc * PADN + p + (p >> 4)); };
+        auto xi = [&](int p) -> int {
+            if constexpr (COLS) return p * TPB + loc;
+            else if constexpr (SWZ) return loc * N + pipe_swz(p);
+            else return loc * PADN + p + (p >> 4);
+        };
         #pragma unroll
         for (int m = 0; m < M; m++){
             int j = t + m * TT;
@@ -184,7 +204,7 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
             }
         }
         if (TO_XCH) __syncthreads();
-        pstage<T, N, TPB, S + 1, FWD, COLS, POST, SEND>(t, loc, xch, tw, v, ld0, st);
+        pstage<T, N, TPB, S + 1, FWD, COLS, POST, SEND, SWZ>(t, loc, xch, tw, v, ld0, st);
     }
 }
 
@@ -211,8 +231,11 @@ __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool
 }
 
 // DF: complex<double> tiles transformed in double-float arithmetic (c2c kinds).
+#ifndef GBFFT_DF_MIN_CTAS
+#define GBFFT_DF_MIN_CTAS 1
+#endif
 template<typename T, int N, int KIND, bool COLS, int LOADER, bool DF = false>
-__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, DF))
+__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, DF), DF ? GBFFT_DF_MIN_CTAS : 1)
 k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
     static_assert(!DF || ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && sizeof(T) == 8),
@@ -359,7 +382,7 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
         }
 
         C *tb = tiles + b * TILE;
-        C *xch = COLS ? tb : xline;
+        C *xch = (COLS || DF) ? tb : xline;
         long long blk, c0;
         tile_origin(tile, blk, c0);
         // transforms of this thread's unit
@@ -431,20 +454,10 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
             D const *twd = reinterpret_cast<D const*>(P.tw);
             D vd[16];
             C *out = reinterpret_cast<C*>(P.out);
-            if (!COLS && LOADER == LD_BULK && P.bulk_store){
-                auto st = [&](int p, D x){ tb[loc * N + p] = back(x); };
-                pstage<df, N, TPB, 0, FWD, COLS, false>(t, loc, xd, twd, vd, ld0, st);
-                fence_proxy_async_smem();
-                __syncthreads();
-                if (tid == 0){
-                    long long lines = ((long long)TPB < P.G - c0) ? (long long)TPB : (P.G - c0);
-                    bulk_s2g(out + base_of_fast(Lo, c0), tb, (uint32_t)(lines * N * sizeof(C)));
-                    bulk_commit();
-                }
-            } else {
-                auto st = [&](int p, D x){ if (va) out[oa + p * oes] = back(x); };
-                pstage<df, N, TPB, 0, FWD, COLS, false>(t, loc, xd, twd, vd, ld0, st);
-            }
+            // the exchange is the tile buffer (swizzled for line tiles), so
+            // the last stage stores straight to global memory
+            auto st = [&](int p, D x){ if (va) out[oa + p * oes] = back(x); };
+            pstage<df, N, TPB, 0, FWD, COLS, false, pipe_nstages(N), !COLS>(t, loc, xd, twd, vd, ld0, st);
             (void)v;
         } else if constexpr (KIND == PK_C2C_FWD || KIND == PK_C2C_BWD){
             auto ld0 = [&](int p) -> C { return COLS ? tb[p * TPB + loc] : tb[loc * N + p]; };

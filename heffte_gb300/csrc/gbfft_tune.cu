@@ -11,6 +11,7 @@
 // driver and library versions): a later run loads the file and skips what was
 // measured, so an interrupted tuning resumes where it stopped.
 #include "gbfft_batch.h"
+#include <algorithm>
 #include <cstdio>
 #include <fstream>
 #include <sstream>
@@ -107,10 +108,13 @@ int tune_load(std::string const &path){
 
 // Times one candidate inside the batched kernel it is tuned for: a batch of
 // boxes whose three sides are all N (the batch reads the candidate from the
-// table), r2c forward + backward.
-static double time_in_batch(cudaStream_t s, int N, int prec, void *in, void *out, void *work, int nbox){
+// table), r2c forward + backward, with the values per thread the candidate
+// runs at (8 for radices up to 8, else 16).
+static double time_in_batch(cudaStream_t s, int N, int prec, void *in, void *out, void *work, int nbox, int values){
     std::vector<std::array<int, 3>> sizes(nbox, std::array<int, 3>{N, N, N});
-    auto b = make_batch(PK_R2C, prec, sizes, s);
+    BatchConfig c;
+    c.values = values;
+    auto b = make_batch(PK_R2C, prec, sizes, s, c);
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");
@@ -155,12 +159,19 @@ int tune_lengths(std::vector<int> const &lengths, int prec, cudaStream_t s, std:
             std::shared_ptr<Fft1D> f;
             try { f = get_fft1d(N, rad); } catch (Error const &){ continue; }
             if (f->plan.T > 256) continue;
-            int deft = std::max(1, 256 / f->plan.T);
+            int const values = std::all_of(rad.begin(), rad.end(), [](int r){ return r <= 8; }) ? 8 : 16;
+            int T = 1;
+            for (int i = 0; i < f->plan.nstages; i++){
+                int per = values / f->plan.st[i].R;
+                T = std::max(T, (f->plan.st[i].NR + per - 1) / per);
+            }
+            if (T > 256) continue;
+            int deft = std::max(1, 256 / T);
             {
                 std::lock_guard<std::mutex> lk(g_mu);
                 g_table[{prec, N}] = TuneChoice{rad, deft, 0};
             }
-            double us = time_in_batch(s, N, prec, in, out, work, nbox);
+            double us = time_in_batch(s, N, prec, in, out, work, nbox, values);
             if (us < best.us){ best.us = us; best.radices = rad; best.tpb = deft; }
         }
         cudaFree(in);

@@ -341,17 +341,22 @@ int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *inpu
  * default 0) > 0 queues the boxes in groups of about that many MB of
  * spectrum with each group's passes two groups apart, so a box's data stays
  * in L2 from one pass to the next (0: pass 0 of every box, then pass 1, then
- * pass 2).  Results are the same for every shape.  configure() rebuilds the
- * batch with a shape; autotune() times forward (input -> output) + backward
- * (output -> back, with workspace) `reps` times for every shape (groups of
- * 0, 16, 32 MB x prefetch on / off x 48, 32, 24 KB), keeps the fastest, and
- * returns it with its ms per forward + backward; it overwrites output, back
- * and workspace, and leaves input as it was. */
-int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch batch, int prefetch, int tile_kb, int group_mb);
-int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch batch, int *prefetch, int *tile_kb, int *group_mb);
+ * pass 2); values (0, 8 or 16, default 0) is the number of complex values
+ * each thread holds: 8 runs radix plans up to 8 with fewer registers and
+ * needs box sides whose prime factors are at most 7, 16 runs any plan, 0
+ * picks 8 where the sides allow it.  Results agree for every shape (to
+ * rounding: the radix plan may differ).  configure() rebuilds the batch with
+ * a shape; config() reports it (values: the one in use); autotune() times
+ * forward (input -> output) + backward (output -> back, with workspace)
+ * `reps` times for every shape (16 / 8 values x groups of 0, 16 MB x
+ * prefetch on / off x 48, 32, 24 KB), keeps the fastest, and returns it with
+ * its ms per forward + backward; it overwrites output, back and workspace,
+ * and leaves input as it was. */
+int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch batch, int prefetch, int tile_kb, int group_mb, int values);
+int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch batch, int *prefetch, int *tile_kb, int *group_mb, int *values);
 int heffte_gb300_boxbatch_autotune(heffte_gb300_boxbatch batch, const void *input, void *output, void *back,
                                    void *workspace, int reps, int *prefetch, int *tile_kb, int *group_mb,
-                                   double *ms);
+                                   int *values, double *ms);
 
 /* No reference counterpart.  Clock budget (GPU clocks, >= 0) after which the
  * batch kernel's wait for another CTA's pass of the same box gives up, records

@@ -133,19 +133,21 @@ def test_dependency_wait_gives_up_and_the_next_call_is_correct(gb):
     assert gb.device_status() == 0
 
 
-@pytest.mark.parametrize("prefetch,tile_kb,group_mb", [(1, 48, 0), (0, 48, 0), (1, 24, 0), (1, 32, 0), (0, 24, 0),
-                                                      (0, 48, 1), (1, 32, 2), (0, 24, 16)])
-def test_batch_launch_shapes_give_the_same_result(gb, prefetch, tile_kb, group_mb):
+@pytest.mark.parametrize("prefetch,tile_kb,group_mb,values", [(1, 48, 0, 16), (0, 48, 0, 16), (1, 24, 0, 16),
+                                                             (1, 32, 0, 8), (0, 24, 0, 8), (0, 48, 1, 8),
+                                                             (1, 32, 2, 16), (0, 24, 16, 8), (1, 48, 0, 8)])
+def test_batch_launch_shapes_give_the_same_result(gb, prefetch, tile_kb, group_mb, values):
     """Every launch shape (the next tile copied ahead into shared memory or
     not; tile bounds that change the CTAs per SM; pass-major queue or boxes in
-    groups, 1 and 2 MB groups making many groups of a few boxes) against the
-    oracle, r2c forward and the backward round trip, float and double sides."""
-    rng = np.random.default_rng(31 + tile_kb + group_mb)
+    groups, 1 and 2 MB groups making many groups of a few boxes; 16 or 8
+    values per thread) against the oracle, r2c forward and the backward round
+    trip, float and double sides."""
+    rng = np.random.default_rng(31 + tile_kb + group_mb + values)
     sizes = _sizes(rng, 30, SIDES)
     for prec in (0, 1):
         b = gb.boxbatch(gb.kind.r2c, sizes, prec)
-        b.configure(prefetch, tile_kb, group_mb)
-        assert b.config() == (prefetch, tile_kb, group_mb)
+        b.configure(prefetch, tile_kb, group_mb, values)
+        assert b.config() == (prefetch, tile_kb, group_mb, values)
         rdt, cdt = (np.float32, torch.complex64) if prec == 0 else (np.float64, torch.complex128)
         x = rng.standard_normal(b.input_size()).astype(rdt)
         xin = torch.from_numpy(x).cuda()
@@ -175,8 +177,9 @@ def test_batch_autotune_keeps_a_correct_shape(gb):
     y = torch.empty_like(xin)
     z = torch.empty_like(xin)
     w = torch.empty(b.workspace_size(), dtype=torch.complex64, device="cuda")
-    pf, kb, gm, ms = b.autotune(xin, y, z, w, reps=2)
-    assert (pf, kb, gm) == b.config() and pf in (0, 1) and kb in (24, 32, 48) and gm in (0, 16, 32) and ms > 0
+    pf, kb, gm, vals, ms = b.autotune(xin, y, z, w, reps=2)
+    assert (pf, kb, gm, vals) == b.config() and pf in (0, 1) and kb in (24, 32, 48) and gm in (0, 16)
+    assert vals in (8, 16) and ms > 0
     assert torch.equal(xin.cpu(), torch.from_numpy(x))      # the input is left as it was
     b.forward(xin, y)
     yh = y.cpu().numpy()
