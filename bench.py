@@ -508,8 +508,8 @@ WORKLOADS = {
     "batch256prefetch": ("batch", "prefetch", 0),
     # the same queued in groups of 16 MB of boxes, each group's passes two groups apart (L2-resident)
     "batch256grouped": ("batch", "grouped", 0),
-    # the same with 16 values per thread (radix-16 plans; the default holds 8)
-    "batch256values16": ("batch", "values16", 0),
+    # the same with 8 values per thread (radix plans up to 8; the default holds 16)
+    "batch256values8": ("batch", "values8", 0),
     # the same boxes as a loop over one fft3d_r2c plan per box (how the reference runs them)
     "batch256loop": ("batch", "loop", 0),
     # learned plan selection on the 2000 measured shapes (tests/golden/selector_timings.npz)
@@ -586,7 +586,7 @@ def run_batch_workload(name, steps, warmup, tune_cache=None):
     if tune_cache == "loop":
         return run_batch_loop(name, sizes, steps, warmup)
     # launch shapes other than the default (prefetch, tile KB, group MB)
-    fixed = {"prefetch": (1, 48, 0, 0), "grouped": (0, 48, 16, 0), "values16": (0, 48, 0, 16)}.get(tune_cache)
+    fixed = {"prefetch": (1, 48, 0, 0), "grouped": (0, 48, 16, 0), "values8": (0, 48, 0, 8)}.get(tune_cache)
     if fixed:
         tune_cache = None
     plans = None
@@ -853,7 +853,7 @@ def run_workload(name, steps, warmup):
         out["double_arithmetic"] = arith
         return out
     if kind == "batch":
-        cache = size if size in ("loop", "prefetch", "grouped", "values16") else None
+        cache = size if size in ("loop", "prefetch", "grouped", "values8") else None
         if size == "tuned":
             import tempfile
             cache = os.path.join(tempfile.mkdtemp(), "tune.tsv")

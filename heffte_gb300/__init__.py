@@ -545,7 +545,7 @@ class boxbatch:
     def configure(self, prefetch=0, tile_kb=48, group_mb=0, values=0):
         """Launch shape: prefetch of each CTA's next tile, tile bound in KB,
         queue order (boxes in L2-sized groups of group_mb MB, 0: pass-major),
-        complex values per thread (8, 16, 0: 8 where the sides allow it)."""
+        complex values per thread (8, 16; 0: 16)."""
         check(lib().heffte_gb300_boxbatch_configure(self._h, int(prefetch), int(tile_kb), int(group_mb), int(values)))
 
     def config(self):

@@ -41,7 +41,7 @@ struct BatchBufs { void const *in; void *out; void *work; };
 // passes two groups apart (its data stays in L2 between them), 0 queues
 // pass 0 of every box, then pass 1, then pass 2; values: complex values each
 // thread holds (8: radix plans up to 8, fewer registers, box sides with prime
-// factors up to 7; 16: any plan; 0: 8 where the sides allow it).
+// factors up to 7; 16 or 0: any plan).
 struct BatchConfig {
     int prefetch = 0;
     int tile_kb = 48;

@@ -203,11 +203,17 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
             __syncthreads();
             if (s_pf_next){
                 TileCopy const tc = s_copy;
-                int const cpr = tc.rowbytes >> 4;
-                long long const total = (long long)tc.rows * cpr;
-                for (long long c = tid; c < total; c += blockDim.x){
-                    int const r = (int)(c / cpr), k = (int)(c - (long long)r * cpr);
+                // 16-byte chunk c = r * cpr + k of the tile, this thread's
+                // chunks tid, tid + blockDim, ...: (r, k) stepped without a
+                // division per chunk
+                int const cpr = tc.rowbytes >> 4, nt = (int)blockDim.x;
+                int const step_r = nt / cpr, step_k = nt - step_r * cpr;
+                int r = tid / cpr, k = tid - (tid / cpr) * cpr;
+                for (; r < tc.rows; ){
                     cp_async_cg16(pfbuf + (long long)r * tc.dststride + 16 * k, tc.src + r * tc.srcstride + 16 * k);
+                    r += step_r;
+                    k += step_k;
+                    if (k >= cpr){ k -= cpr; r++; }
                 }
                 asm volatile("cp.async.commit_group;" ::: "memory");
             }

@@ -231,11 +231,21 @@ __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool
 }
 
 // DF: complex<double> tiles transformed in double-float arithmetic (c2c kinds).
+// CTAs per SM the double-float kernels are compiled for (their register
+// budget): 16 values per thread need about 128 registers, 168 unbounded; at
+// six CTAs (80 registers) lengths up to 256 spill little and gain (256^3 Z2Z
+// forward + backward 2.39 ms against 2.58 at four), longer ones spill more
+// and lose (512^3: 31.1 ms at six, 21.3 at five, 20.0 at four, 35.7
+// unbounded); 256-thread CTAs (4096 points) two.
 #ifndef GBFFT_DF_MIN_CTAS
-#define GBFFT_DF_MIN_CTAS 1
+#define GBFFT_DF_MIN_CTAS 0
 #endif
+__host__ __device__ constexpr int pipe_df_min_ctas(int N, int threads){
+    return GBFFT_DF_MIN_CTAS > 0 ? GBFFT_DF_MIN_CTAS : (threads > 128 ? 2 : (N <= 256 ? 6 : 4));
+}
 template<typename T, int N, int KIND, bool COLS, int LOADER, bool DF = false>
-__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, DF), DF ? GBFFT_DF_MIN_CTAS : 1)
+__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, DF),
+                                  DF ? pipe_df_min_ctas(N, pipe_threads(N, sizeof(c_t<T>), COLS, DF)) : 1)
 k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
     static_assert(!DF || ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && sizeof(T) == 8),

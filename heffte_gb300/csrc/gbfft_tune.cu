@@ -108,8 +108,7 @@ int tune_load(std::string const &path){
 
 // Times one candidate inside the batched kernel it is tuned for: a batch of
 // boxes whose three sides are all N (the batch reads the candidate from the
-// table), r2c forward + backward, with the values per thread the candidate
-// runs at (8 for radices up to 8, else 16).
+// table), r2c forward + backward, at `values` values per thread.
 static double time_in_batch(cudaStream_t s, int N, int prec, void *in, void *out, void *work, int nbox, int values){
     std::vector<std::array<int, 3>> sizes(nbox, std::array<int, 3>{N, N, N});
     BatchConfig c;
@@ -159,19 +158,12 @@ int tune_lengths(std::vector<int> const &lengths, int prec, cudaStream_t s, std:
             std::shared_ptr<Fft1D> f;
             try { f = get_fft1d(N, rad); } catch (Error const &){ continue; }
             if (f->plan.T > 256) continue;
-            int const values = std::all_of(rad.begin(), rad.end(), [](int r){ return r <= 8; }) ? 8 : 16;
-            int T = 1;
-            for (int i = 0; i < f->plan.nstages; i++){
-                int per = values / f->plan.st[i].R;
-                T = std::max(T, (f->plan.st[i].NR + per - 1) / per);
-            }
-            if (T > 256) continue;
-            int deft = std::max(1, 256 / T);
+            int deft = std::max(1, 256 / f->plan.T);
             {
                 std::lock_guard<std::mutex> lk(g_mu);
                 g_table[{prec, N}] = TuneChoice{rad, deft, 0};
             }
-            double us = time_in_batch(s, N, prec, in, out, work, nbox, values);
+            double us = time_in_batch(s, N, prec, in, out, work, nbox, 16);
             if (us < best.us){ best.us = us; best.radices = rad; best.tpb = deft; }
         }
         cudaFree(in);

@@ -343,8 +343,7 @@ int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *inpu
  * in L2 from one pass to the next (0: pass 0 of every box, then pass 1, then
  * pass 2); values (0, 8 or 16, default 0) is the number of complex values
  * each thread holds: 8 runs radix plans up to 8 with fewer registers and
- * needs box sides whose prime factors are at most 7, 16 runs any plan, 0
- * picks 8 where the sides allow it.  Results agree for every shape (to
+ * needs box sides whose prime factors are at most 7, 16 (or 0) runs any plan.  Results agree for every shape (to
  * rounding: the radix plan may differ).  configure() rebuilds the batch with
  * a shape; config() reports it (values: the one in use); autotune() times
  * forward (input -> output) + backward (output -> back, with workspace)
