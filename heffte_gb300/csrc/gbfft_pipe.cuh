@@ -243,10 +243,11 @@ __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool
 __host__ __device__ constexpr int pipe_df_min_ctas(int N, int threads){
     return GBFFT_DF_MIN_CTAS > 0 ? GBFFT_DF_MIN_CTAS : (threads > 128 ? 2 : (N <= 256 ? 6 : 4));
 }
-template<typename T, int N, int KIND, bool COLS, int LOADER, bool DF = false>
-__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, DF),
-                                  DF ? pipe_df_min_ctas(N, pipe_threads(N, sizeof(c_t<T>), COLS, DF)) : 1)
-k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
+// The body of the pipelined kernels; k_pipe (bounded by its thread count
+// alone: the compiler's own register choice) and k_pipe_df (also by the CTAs
+// per SM above) are its two entry points.
+template<typename T, int N, int KIND, bool COLS, int LOADER, bool DF>
+__device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const &tmap){
     using C = c_t<T>;
     static_assert(!DF || ((KIND == PK_C2C_FWD || KIND == PK_C2C_BWD) && sizeof(T) == 8),
                   "double-float arithmetic serves the complex<double> c2c kinds");
@@ -659,6 +660,19 @@ k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
     }
     // the last bulk stores must be complete before the CTA's shared memory goes
     if (LOADER == LD_BULK && P.bulk_store && tid == 0) bulk_wait<0>();
+}
+
+template<typename T, int N, int KIND, bool COLS, int LOADER>
+__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS))
+k_pipe(PipeParams P, const __grid_constant__ CUtensorMap tmap){
+    pipe_body<T, N, KIND, COLS, LOADER, false>(P, tmap);
+}
+
+template<typename T, int N, int KIND, bool COLS, int LOADER>
+__global__ void __launch_bounds__(pipe_threads(N, sizeof(c_t<T>), COLS, true),
+                                  pipe_df_min_ctas(N, pipe_threads(N, sizeof(c_t<T>), COLS, true)))
+k_pipe_df(PipeParams P, const __grid_constant__ CUtensorMap tmap){
+    pipe_body<T, N, KIND, COLS, LOADER, true>(P, tmap);
 }
 
 } // namespace gbfft

@@ -78,7 +78,10 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
     } else {
         if (Li.dist != 1 || (IN_ES != 8 && IN_ES != 16) || (base % IN_ES)) return false;
     }
-    auto kern = k_pipe<T, N, KIND, COLS, LOADER, DF>;
+    auto kern = []{
+        if constexpr (DF) return k_pipe_df<T, N, KIND, COLS, LOADER>;
+        else return k_pipe<T, N, KIND, COLS, LOADER>;
+    }();
     static std::atomic<unsigned long long> ready{0};
     static int blocks_per_sm[64] = {0};
     int dev = 0;
