@@ -18,6 +18,7 @@
 // stage (or the fused post-processing of r2c / DCT) stores straight to HBM.
 #pragma once
 #include <cuda.h>
+#include <type_traits>
 #include "gbfft_common.cuh"
 #include "gbfft_ptx.cuh"
 
@@ -64,8 +65,16 @@ __host__ __device__ constexpr int cilog2(int v){
     while ((1 << l) < v) l++;
     return l;
 }
-__host__ __device__ constexpr int pipe_pe(int N){ return (N < 16) ? N : 16; }     // values per thread
-__host__ __device__ constexpr int pipe_tt(int N){ return N / pipe_pe(N); }        // threads per unit
+// values per thread: 16, or for the double-float kernels 8 where every radix
+// of the plan is at most 8 (32, 64, 512: half the registers and half the
+// unrolled code per stage, twice the threads)
+__host__ __device__ constexpr bool pipe_radices_upto8(int N){
+    return N == 32 || N == 64 || N == 512;
+}
+__host__ __device__ constexpr int pipe_pe(int N, bool df = false){
+    return (N < 16) ? N : ((df && pipe_radices_upto8(N)) ? 8 : 16);
+}
+__host__ __device__ constexpr int pipe_tt(int N, bool df = false){ return N / pipe_pe(N, df); }   // threads per unit
 __host__ __device__ constexpr int pipe_padn(int N){ return N + N / 16 + 1; }
 __host__ __device__ constexpr bool pipe_paired(int kind){ return kind >= PK_R2C_FWD; }
 // units (complex transforms or real pairs) per tile.  df: the double-float
@@ -77,7 +86,8 @@ __host__ __device__ constexpr bool pipe_paired(int kind){ return kind >= PK_R2C_
 // a 512^3 complex<double> forward + backward).
 __host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols, bool df = false){
     if (df){
-        int tpb = (128 / pipe_tt(N) > 1) ? 128 / pipe_tt(N) : 1;
+        int const tt = pipe_tt(N, true), target = pipe_radices_upto8(N) ? 256 : 128;
+        int tpb = (target / tt > 1) ? target / tt : 1;
         while (tpb > 1 && (N + 4) * tpb * csize > 64 * 1024) tpb /= 2;
         return tpb;
     }
@@ -161,7 +171,8 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
     constexpr int NS = pipe_nstages(N);
     if constexpr (S < SEND){
         constexpr int R = pipe_radix(N, S), Ns = pipe_ns(N, S), TWO = pipe_twoff(N, S);
-        constexpr int NR = N / R, TT = pipe_tt(N), M = pipe_pe(N) / R, PADN = pipe_padn(N);
+        constexpr bool DFT = std::is_same<T, df>::value;
+        constexpr int NR = N / R, TT = pipe_tt(N, DFT), M = pipe_pe(N, DFT) / R, PADN = pipe_padn(N);
         constexpr bool LAST = (S == NS - 1);
         constexpr bool TO_XCH = !LAST || POST;
         constexpr int LNS = cilog2(Ns), LNSR = cilog2(Ns * R);
@@ -227,7 +238,7 @@ __device__ __forceinline__ void cp_async_commit(){ asm volatile("cp.async.commit
 template<int NG> __device__ __forceinline__ void cp_async_wait(){ asm volatile("cp.async.wait_group %0;" :: "n"(NG) : "memory"); }
 
 __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool df = false){
-    return pipe_tpb(N, csize, cols, df) * pipe_tt(N);
+    return pipe_tpb(N, csize, cols, df) * pipe_tt(N, df);
 }
 
 // DF: complex<double> tiles transformed in double-float arithmetic (c2c kinds).
@@ -235,13 +246,17 @@ __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool
 // budget): 16 values per thread need about 128 registers, 168 unbounded; at
 // six CTAs (80 registers) lengths up to 256 spill little and gain (256^3 Z2Z
 // forward + backward 2.39 ms against 2.58 at four), longer ones spill more
-// and lose (512^3: 31.1 ms at six, 21.3 at five, 20.0 at four, 35.7
-// unbounded); 256-thread CTAs (4096 points) two.
+// and lose (512^3 with 16 values: 31.1 ms at six, 21.3 at five, 20.0 at
+// four, 35.7 unbounded); 256-thread CTAs of 16 values (4096 points) two.
+// With 8 values per thread (32, 64, 512 points; 256-thread CTAs) four CTAs
+// fit in 64 registers without spilling: 512^3 16.4 ms (three: 17.2, five:
+// 16.7).
 #ifndef GBFFT_DF_MIN_CTAS
 #define GBFFT_DF_MIN_CTAS 0
 #endif
 __host__ __device__ constexpr int pipe_df_min_ctas(int N, int threads){
-    return GBFFT_DF_MIN_CTAS > 0 ? GBFFT_DF_MIN_CTAS : (threads > 128 ? 2 : (N <= 256 ? 6 : 4));
+    return GBFFT_DF_MIN_CTAS > 0 ? GBFFT_DF_MIN_CTAS
+                                 : (pipe_radices_upto8(N) ? 4 : (threads > 128 ? 2 : (N <= 256 ? 6 : 4)));
 }
 // The body of the pipelined kernels; k_pipe (bounded by its thread count
 // alone: the compiler's own register choice) and k_pipe_df (also by the CTAs
@@ -253,7 +268,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                   "double-float arithmetic serves the complex<double> c2c kinds");
     constexpr bool PAIRED = pipe_paired(KIND);
     constexpr int TPB = pipe_tpb(N, sizeof(C), COLS, DF);
-    constexpr int TT = pipe_tt(N);
+    constexpr int TT = pipe_tt(N, DF);
     constexpr int NT = TPB * TT;
     constexpr int TILE = pipe_tile_elems(N, TPB, KIND);   // complex elements per buffer
     constexpr int H = N / 2 + 1;
