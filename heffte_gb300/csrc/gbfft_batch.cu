@@ -107,6 +107,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     if (config.group_mb < 0 || config.group_mb > 4096) throw Error(ST_INVALID, "group size must be 0 to 4096 MB");
     if (config.values != 0 && config.values != 8 && config.values != 16)
         throw Error(ST_INVALID, "values per thread must be 0 (automatic), 8 or 16");
+    if (config.tuned_plans != 0 && config.tuned_plans != 1) throw Error(ST_INVALID, "tuned_plans must be 0 or 1");
     auto b = std::make_unique<Batch>();
     b->kind = kind; b->prec = prec; b->sizes = sizes; b->stream = stream;
     b->config = config;
@@ -147,7 +148,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     std::vector<void const*> tws;
     std::vector<int> tpb_hint;
     for (int N : lens){
-        TuneChoice tc = tuned_choice(N, prec);
+        TuneChoice tc = config.tuned_plans ? tuned_choice(N, prec) : TuneChoice{};
         std::vector<int> rad = tc.radices;
         int hint = tc.tpb;
         if (values == 8){
@@ -379,9 +380,10 @@ static void build_graph(Batch &b, bool fwd){
     (fwd ? b.fwd_knode : b.bwd_knode) = knode;
 }
 
-// Times forward + backward of every launch shape (16 or 8 values per thread,
-// queue order pass-major or in groups of 16 MB, prefetch on / off, tile
-// bounds of 48, 32 and 24 KB: 2 to 5 CTAs per SM) on the caller's buffers
+// Times forward + backward of every launch shape (the tuned radix plans or
+// the default ones, 16 or 8 values per thread, queue order pass-major or in
+// groups of 16 MB, prefetch on / off, tile bounds of 48, 32 and 24 KB: 2 to 5
+// CTAs per SM) on the caller's buffers
 // and leaves `b` built with the fastest; the untuned default is a candidate,
 // so tuning never makes the batch slower than it was (within the timing noise).
 BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out, void *back, void *work, int reps,
@@ -398,17 +400,19 @@ BatchConfig autotune_batch(std::unique_ptr<Batch> &b, void const *in, void *out,
     check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
     check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
     std::vector<BatchConfig> shapes;
-    for (int vals : {16, 8})
-        for (int gm : {0, 16})
-            for (int pf : {0, 1})
-                for (int kb : {48, 32, 24}){
-                    BatchConfig c;
-                    c.prefetch = pf;
-                    c.tile_kb = kb;
-                    c.group_mb = gm;
-                    c.values = vals;
-                    shapes.push_back(c);
-                }
+    for (int tp : {1, 0})
+        for (int vals : {16, 8})
+            for (int gm : {0, 16})
+                for (int pf : {0, 1})
+                    for (int kb : {48, 32, 24}){
+                        BatchConfig c;
+                        c.prefetch = pf;
+                        c.tile_kb = kb;
+                        c.group_mb = gm;
+                        c.values = vals;
+                        c.tuned_plans = tp;
+                        shapes.push_back(c);
+                    }
     {
         for (BatchConfig const &c : shapes){
             std::unique_ptr<Batch> cand;

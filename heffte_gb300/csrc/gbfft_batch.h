@@ -47,6 +47,7 @@ struct BatchConfig {
     int tile_kb = 48;
     int group_mb = 0;
     int values = 0;
+    int tuned_plans = 1;    // radix plans from the tuning table (1) or the defaults (0)
 };
 struct BatchUnit;   // one 1-D pass of one box (gbfft_batch.cu)
 

@@ -347,10 +347,12 @@ int heffte_gb300_boxbatch_backward(heffte_gb300_boxbatch batch, const void *inpu
  * rounding: the radix plan may differ).  configure() rebuilds the batch with
  * a shape; config() reports it (values: the one in use); autotune() times
  * forward (input -> output) + backward (output -> back, with workspace)
- * `reps` times for every shape (16 / 8 values x groups of 0, 16 MB x
- * prefetch on / off x 48, 32, 24 KB), keeps the fastest, and returns it with
- * its ms per forward + backward; it overwrites output, back and workspace,
- * and leaves input as it was. */
+ * `reps` times for every shape (the tuning table's radix plans or the
+ * default ones x 16 / 8 values x groups of 0, 16 MB x prefetch on / off x
+ * 48, 32, 24 KB), keeps the fastest (the untuned default is a candidate, so
+ * tuning never makes a batch slower beyond timing noise), and returns it
+ * with its ms per forward + backward; it overwrites output, back and
+ * workspace, and leaves input as it was. */
 int heffte_gb300_boxbatch_configure(heffte_gb300_boxbatch batch, int prefetch, int tile_kb, int group_mb, int values);
 int heffte_gb300_boxbatch_config(heffte_gb300_boxbatch batch, int *prefetch, int *tile_kb, int *group_mb, int *values);
 int heffte_gb300_boxbatch_autotune(heffte_gb300_boxbatch batch, const void *input, void *output, void *back,
