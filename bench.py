@@ -494,6 +494,8 @@ WORKLOADS = {
     "z2z256": ("c2c", (256, 256, 256), 1),
     "z2z256fp64": ("c2c", (256, 256, 256), 1, False, "fp64"),
     "z2z256df": ("c2c", (256, 256, 256), 1, False, "double-float"),
+    # small case (256 MiB, above L2) of the 512-point double-float passes, for ncu captures
+    "z2z512x512x64df": ("c2c", (512, 512, 64), 1, False, "double-float"),
     # the FP64 rate of this GPU: cuBLAS DGEMM 8192^3 through torch (burst)
     "fp64peak": ("fp64peak", None, 1),
     # small case (256 MiB, above L2) for ncu captures of the c2c pass kernels
