@@ -352,7 +352,7 @@ def ours(args, rank, world, local_rank):
                      # DRAM read+write bytes per launch of the column pass kernel: not measured
                      # in this run, but taken from one ncu capture of this command
                      # (profiles/k_pipe_c2c_512cube_fp32.md); traffic_source says so in the line
-                     "traffic": 2.083e9 if (n == 512 and prec == 0) else None,
+                     "traffic": 2.086e9 if (n == 512 and prec == 0) else None,
                      "traffic_source": ("ncu capture of this command (dram__bytes_read.sum + "
                                         "dram__bytes_write.sum per launch), profiles/k_pipe_c2c_512cube_fp32.md; "
                                         "not measured in this run") if (n == 512 and prec == 0) else None,
