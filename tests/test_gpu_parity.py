@@ -436,7 +436,7 @@ def test_power_of_two_kernel_variants(gb, variant, prec):
     try:
         rng = np.random.default_rng(variant + 2 * prec)
         for size in [(2, 4, 8), (16, 32, 64), (128, 16, 32), (256, 8, 16), (512, 16, 32), (32, 1024, 2),
-                     (2048, 2, 16), (4096, 2, 4), (64, 64, 64)]:
+                     (2048, 2, 16), (4096, 2, 4), (64, 64, 64), (50, 512, 2), (14, 2048, 2), (6, 4096, 2)]:
             n = int(np.prod(size))
             x = rand_c(rng, n, prec)
             for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 1, 0), (2, 1, 0)), ((1, 0, 2), (0, 2, 1))]:
