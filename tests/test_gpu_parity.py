@@ -427,11 +427,13 @@ def test_r2r_prepost_location_layer_bit_exact(gb, rkind, prec):
         assert host(out).tobytes() == want.tobytes(), (rkind, step)
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("prec", [0, 1])
 def test_power_of_two_kernel_variants(gb, variant, prec):
-    """Both kernel families (generic runtime-radix, pipelined bulk-copy) on the
-    power-of-two lengths, line and column layouts, in and out of place."""
+    """Every kernel family (0: the default pipelined kernels with tensor-map
+    column tiles; 1, 2: generic runtime-radix, pipelined bulk-copy) on the
+    power-of-two lengths, line and column layouts (partial wide column tiles
+    of 512, 2048 and 4096 points), in and out of place."""
     gb.set_kernel_variant(variant)
     try:
         rng = np.random.default_rng(variant + 2 * prec)
