@@ -35,7 +35,8 @@ def _run(gb, x, size, io=(0, 1, 2), oo=(0, 1, 2), reorder=0):
     return y.cpu().numpy(), z.cpu().numpy()
 
 
-@pytest.mark.parametrize("size", [(16, 32, 64), (64, 16, 128), (128, 256, 32), (2048, 16, 8), (512, 8, 1024)])
+@pytest.mark.parametrize("size", [(16, 32, 64), (64, 16, 128), (128, 256, 32), (2048, 16, 8), (512, 8, 1024),
+                                  (4096, 4, 2), (2, 4, 8), (8, 1024, 4), (32, 512, 6)])
 def test_double_float_against_fp64(double_float, size):
     gb = double_float
     rng = np.random.default_rng(sum(size))
