@@ -369,10 +369,10 @@ bool encode_column_tmap(void *tmap, void const *base, int esize, long long count
     return true;
 }
 
-std::vector<int> pipe_radices(int N){
+std::vector<int> pipe_radices(int N, bool df){
     if (N < 2 || N > 4096 || (N & (N - 1))) return {};
     std::vector<int> r;
-    for (int s = 0; s < pipe_nstages(N); s++) r.push_back(pipe_radix(N, s));
+    for (int s = 0; s < pipe_nstages(N, df); s++) r.push_back(pipe_radix(N, s, df));
     return r;
 }
 
@@ -423,7 +423,8 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
         return launch_pipe_f32_r2r(s, kind, f.N, cols, a);
     }
     if (c2c && double_arithmetic() == DA_DOUBLE_FLOAT){
-        a.tw = f.twiddles_df(s);
+        // the double-float kernels run their own plan (radices up to 8)
+        a.tw = get_fft1d(f.N, pipe_radices(f.N, true))->twiddles_df(s);
         return launch_pipe_df64_c2c(s, kind, f.N, cols, a);
     }
     if (c2c) return launch_pipe_f64_c2c(s, kind, f.N, cols, a);

@@ -233,7 +233,8 @@ void launch_pointwise(cudaStream_t s, int prec, long long n, void *a, void const
 struct CUtensorMap_st;
 bool encode_column_tmap(void *tmap, void const *base, int csize, long long count, long long N, long long blocks,
                         long long estride, long long bstride, int tpb, int boxr, int *swap);
-std::vector<int> pipe_radices(int N);   // empty if N has no pipelined kernel
+// empty if N has no pipelined kernel; df: the plan of the double-float kernels
+std::vector<int> pipe_radices(int N, bool df = false);
 
 // Kernel family selection (process-wide): 0 automatic, 1 generic runtime-radix
 // kernels only, 2 pipelined kernels wherever they apply.

@@ -29,11 +29,32 @@ enum { PK_C2C_FWD = 0, PK_C2C_BWD = 1, PK_R2C_FWD = 2, PK_C2R_BWD = 3, PK_R2R_FW
 // loaders
 enum { LD_TENSOR = 0, LD_BULK = 1, LD_CPASYNC = 2 };
 
-// Radix plan of the pipelined kernels: at most 16 values per thread.
-__host__ __device__ constexpr int pipe_nstages(int N){
+// Radix plan of the pipelined kernels: at most 16 values per thread.  The
+// double-float kernels (df) use radices up to 8 (8 values per thread):
+// radix-8 stages, the rest as 4 or 4 x 4.
+__host__ __device__ constexpr int pipe_df_radix(int N, int s){
+    switch (N){
+        case 2: return 2;
+        case 4: return 4;
+        case 8: return 8;
+        case 16: return 4;
+        case 32: return (s == 0) ? 8 : 4;
+        case 64: return 8;
+        case 128: return (s == 0) ? 8 : 4;
+        case 256: return (s < 2) ? 8 : 4;
+        case 512: return 8;
+        case 1024: return (s < 2) ? 8 : 4;
+        case 2048: return (s < 3) ? 8 : 4;
+        case 4096: return 8;
+        default: return 0;
+    }
+}
+__host__ __device__ constexpr int pipe_nstages(int N, bool df = false){
+    if (df) return (N <= 8) ? 1 : ((N <= 64) ? 2 : ((N <= 512) ? 3 : 4));
     return (N <= 16) ? 1 : ((N <= 256) ? 2 : 3);
 }
-__host__ __device__ constexpr int pipe_radix(int N, int s){
+__host__ __device__ constexpr int pipe_radix(int N, int s, bool df = false){
+    if (df) return pipe_df_radix(N, s);
     switch (N){
         case 2: return 2;
         case 4: return 4;
@@ -50,14 +71,14 @@ __host__ __device__ constexpr int pipe_radix(int N, int s){
         default: return 0;
     }
 }
-__host__ __device__ constexpr int pipe_ns(int N, int s){
+__host__ __device__ constexpr int pipe_ns(int N, int s, bool df = false){
     int p = 1;
-    for (int i = 0; i < s; i++) p *= pipe_radix(N, i);
+    for (int i = 0; i < s; i++) p *= pipe_radix(N, i, df);
     return p;
 }
-__host__ __device__ constexpr int pipe_twoff(int N, int s){
+__host__ __device__ constexpr int pipe_twoff(int N, int s, bool df = false){
     int off = 0;
-    for (int i = 1; i < s; i++) off += pipe_ns(N, i) * (pipe_radix(N, i) - 1);
+    for (int i = 1; i < s; i++) off += pipe_ns(N, i, df) * (pipe_radix(N, i, df) - 1);
     return off;
 }
 __host__ __device__ constexpr int cilog2(int v){
@@ -65,28 +86,25 @@ __host__ __device__ constexpr int cilog2(int v){
     while ((1 << l) < v) l++;
     return l;
 }
-// values per thread: 16, or for the double-float kernels 8 where every radix
-// of the plan is at most 8 (32, 64, 512: half the registers and half the
-// unrolled code per stage, twice the threads)
-__host__ __device__ constexpr bool pipe_radices_upto8(int N){
-    return N == 32 || N == 64 || N == 512;
-}
+// values per thread: 16, or 8 for the double-float kernels (their plans
+// have no radix above 8: half the registers and half the unrolled code per
+// stage of 16 values, twice the threads)
 __host__ __device__ constexpr int pipe_pe(int N, bool df = false){
-    return (N < 16) ? N : ((df && pipe_radices_upto8(N)) ? 8 : 16);
+    return df ? ((N < 8) ? N : 8) : ((N < 16) ? N : 16);
 }
 __host__ __device__ constexpr int pipe_tt(int N, bool df = false){ return N / pipe_pe(N, df); }   // threads per unit
 __host__ __device__ constexpr int pipe_padn(int N){ return N + N / 16 + 1; }
 __host__ __device__ constexpr bool pipe_paired(int kind){ return kind >= PK_R2C_FWD; }
 // units (complex transforms or real pairs) per tile.  df: the double-float
 // complex<double> kernels, which are bound by the latency of their FP32
-// dependency chains rather than by memory: CTAs of about 128 threads with
+// dependency chains rather than by memory: CTAs of about 256 threads with
 // one tile slot and no separate exchange buffer (line tiles exchange in the
-// tile buffer, swizzled), so that four or five CTAs share an SM and their
-// warps hide that latency (one slot: 21.7 against 29.0 ms with two slots for
-// a 512^3 complex<double> forward + backward).
+// tile buffer, swizzled), so that shared memory holds several CTAs per SM and
+// their warps hide that latency (one slot: 21.7 against 29.0 ms with two
+// slots for a 512^3 complex<double> forward + backward).
 __host__ __device__ constexpr int pipe_tpb(int N, int csize, bool cols, bool df = false){
     if (df){
-        int const tt = pipe_tt(N, true), target = pipe_radices_upto8(N) ? 256 : 128;
+        int const tt = pipe_tt(N, true), target = 256;
         int tpb = (target / tt > 1) ? target / tt : 1;
         while (tpb > 1 && (N + 4) * tpb * csize > 64 * 1024) tpb /= 2;
         return tpb;
@@ -175,15 +193,15 @@ __host__ __device__ constexpr int pipe_swz(int p){
 // exchange buffer).
 // SWZ: line tiles exchanged in the tile buffer itself (pitch N), element p of
 // a line at pipe_swz(p) (no padding, the bank spread of an XOR swizzle).
-template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST, int SEND = pipe_nstages(N),
-         bool SWZ = false, class LD, class ST>
+template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST,
+         int SEND = pipe_nstages(N, std::is_same<T, df>::value), bool SWZ = false, class LD, class ST>
 __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const *__restrict__ tw,
                                        c_t<T> (&v)[16], LD &ld0, ST &st){
     using C = c_t<T>;
-    constexpr int NS = pipe_nstages(N);
+    constexpr bool DFT = std::is_same<T, df>::value;
+    constexpr int NS = pipe_nstages(N, DFT);
     if constexpr (S < SEND){
-        constexpr int R = pipe_radix(N, S), Ns = pipe_ns(N, S), TWO = pipe_twoff(N, S);
-        constexpr bool DFT = std::is_same<T, df>::value;
+        constexpr int R = pipe_radix(N, S, DFT), Ns = pipe_ns(N, S, DFT), TWO = pipe_twoff(N, S, DFT);
         constexpr int NR = N / R, TT = pipe_tt(N, DFT), M = pipe_pe(N, DFT) / R, PADN = pipe_padn(N);
         constexpr bool LAST = (S == NS - 1);
         constexpr bool TO_XCH = !LAST || POST;
@@ -255,20 +273,16 @@ __host__ __device__ constexpr int pipe_threads(int N, int csize, bool cols, bool
 
 // DF: complex<double> tiles transformed in double-float arithmetic (c2c kinds).
 // CTAs per SM the double-float kernels are compiled for (their register
-// budget): 16 values per thread need about 128 registers, 168 unbounded; at
-// six CTAs (80 registers) lengths up to 256 spill little and gain (256^3 Z2Z
-// forward + backward 2.39 ms against 2.58 at four), longer ones spill more
-// and lose (512^3 with 16 values: 31.1 ms at six, 21.3 at five, 20.0 at
-// four, 35.7 unbounded); 256-thread CTAs of 16 values (4096 points) two.
-// With 8 values per thread (32, 64, 512 points; 256-thread CTAs) four CTAs
-// fit in 64 registers without spilling: 512^3 16.4 ms (three: 17.2, five:
-// 16.7).
+// budget): 1024 threads per SM, 64 registers a thread, which 8 values per
+// thread fit without spilling (512^3 Z2Z forward + backward 16.4 ms; compiled
+// for 3 or 5 CTAs of 256 threads: 17.2, 16.7 ms).  With 16 values per thread
+// (the earlier plans with radix-16 stages) the best budgets were 128 registers
+// (512^3: 20.0 ms; 168 unbounded: 35.7) and 80 for 256 points.
 #ifndef GBFFT_DF_MIN_CTAS
 #define GBFFT_DF_MIN_CTAS 0
 #endif
 __host__ __device__ constexpr int pipe_df_min_ctas(int N, int threads){
-    return GBFFT_DF_MIN_CTAS > 0 ? GBFFT_DF_MIN_CTAS
-                                 : (pipe_radices_upto8(N) ? 4 : (threads > 128 ? 2 : (N <= 256 ? 6 : 4)));
+    return GBFFT_DF_MIN_CTAS > 0 ? GBFFT_DF_MIN_CTAS : ((threads >= 1024) ? 1 : 1024 / threads);
 }
 // The body of the pipelined kernels; k_pipe (bounded by its thread count
 // alone: the compiler's own register choice) and k_pipe_df (also by the CTAs
@@ -495,7 +509,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
             // the exchange is the tile buffer (swizzled for line tiles), so
             // the last stage stores straight to global memory
             auto st = [&](int p, D x){ if (va) out[oa + p * oes] = back(x); };
-            pstage<df, N, TPB, 0, FWD, COLS, false, pipe_nstages(N), !COLS>(t, loc, xd, twd, vd, ld0, st);
+            pstage<df, N, TPB, 0, FWD, COLS, false, pipe_nstages(N, true), !COLS>(t, loc, xd, twd, vd, ld0, st);
             (void)v;
         } else if constexpr (KIND == PK_C2C_FWD || KIND == PK_C2C_BWD){
             auto ld0 = [&](int p) -> C { return COLS ? tb[p * TPB + loc] : tb[loc * N + p]; };
