@@ -241,7 +241,14 @@ __host__ __device__ constexpr long long padded_pitch(long long e){
     return (e >= 65) ? ((e + 7) / 8) * 8 : e + (e & 1);
 }
 
+// 32-bit division where g and count allow it (a 64-bit division is a long
+// instruction sequence, and the generic kernels take this per thread per tile)
 __device__ __forceinline__ long long base_of(Layout const &L, long long g){
+    if (g < 0x7fffffffLL && L.count < 0x7fffffffLL){
+        unsigned const gg = (unsigned)g, c = (unsigned)L.count;
+        unsigned const q = gg / c;
+        return (long long)q * L.bstride + (long long)(gg - q * c) * L.dist;
+    }
     return (g / L.count) * L.bstride + (g % L.count) * L.dist;
 }
 

@@ -249,14 +249,7 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
     }
 }
 
-__device__ __forceinline__ long long base_of_fast(Layout const &L, long long g){
-    if (g < 0x7fffffffLL && L.count < 0x7fffffffLL){
-        unsigned gg = (unsigned)g, c = (unsigned)L.count;
-        unsigned q = gg / c;
-        return (long long)q * L.bstride + (long long)(gg - q * c) * L.dist;
-    }
-    return (g / L.count) * L.bstride + (g % L.count) * L.dist;
-}
+__device__ __forceinline__ long long base_of_fast(Layout const &L, long long g){ return base_of(L, g); }
 
 __device__ __forceinline__ void cp_async_8(void *dst, void const *src, bool valid){
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(smem_u32(dst)), "l"(src), "r"(valid ? 8 : 0) : "memory");
