@@ -1,6 +1,7 @@
 // Shared definitions of the GB300 fft3d backend: complex helpers, the
 // device-side plan of one batched 1-D transform, radix butterflies.
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -199,6 +200,64 @@ __host__ __device__ __forceinline__ cdf cmul(cdf a, cdf b){
 __host__ __device__ __forceinline__ cdf cmulc(cdf a, cdf b){
     cdf r; r.x = df_dot2(a.x, b.x, a.y, b.y); r.y = df_dot2(a.y, b.x, -a.x, b.y); return r;
 }
+// Double-float butterflies of radix 2, 4 and 8 with one renormalisation per
+// output instead of one per addition: inside a butterfly the sums keep the
+// exact sum of the heads (TwoSum) and add the tails without renormalising
+// (8 FP32 operations instead of 11); a pair whose tail is not below half an
+// ulp of its head still represents the value to about 2^-48 of the operand
+// magnitudes (the normwise bound an FFT's error analysis uses), and it is
+// renormalised (FastTwoSum) before a product and on the way out.
+struct dfb {
+    __host__ __device__ static __forceinline__ df add(df a, df b){
+        df const s = df_two_sum(a.hi, b.hi);
+        return df(s.hi, s.lo + (a.lo + b.lo));
+    }
+    __host__ __device__ static __forceinline__ df sub(df a, df b){ return add(a, -b); }
+    __host__ __device__ static __forceinline__ df norm(df a){ return df_fast_two_sum(a.hi, a.lo); }
+    __host__ __device__ static __forceinline__ cdf cadd(cdf a, cdf b){ cdf r; r.x = add(a.x, b.x); r.y = add(a.y, b.y); return r; }
+    __host__ __device__ static __forceinline__ cdf csub(cdf a, cdf b){ cdf r; r.x = sub(a.x, b.x); r.y = sub(a.y, b.y); return r; }
+    __host__ __device__ static __forceinline__ cdf cnorm(cdf a){ cdf r; r.x = norm(a.x); r.y = norm(a.y); return r; }
+    template<bool FWD> __host__ __device__ static __forceinline__ cdf rot(cdf a){
+        cdf r;
+        if (FWD){ r.x = a.y; r.y = -a.x; } else { r.x = -a.y; r.y = a.x; }
+        return r;
+    }
+    // radix 4 in place, outputs not renormalised
+    template<bool FWD> __host__ __device__ static __forceinline__ void r4(cdf *v){
+        cdf const a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        cdf const c = cadd(v[1], v[3]), d = rot<FWD>(csub(v[1], v[3]));
+        v[0] = cadd(a, c); v[2] = csub(a, c);
+        v[1] = cadd(b, d); v[3] = csub(b, d);
+    }
+    template<int R, bool FWD> __host__ __device__ static __forceinline__ void bfly(cdf *v){
+        if constexpr (R == 2){
+            cdf const a = v[0], b = v[1];
+            v[0] = cnorm(cadd(a, b)); v[1] = cnorm(csub(a, b));
+        } else if constexpr (R == 4){
+            r4<FWD>(v);
+            for (int k = 0; k < 4; k++) v[k] = cnorm(v[k]);
+        } else {
+            static_assert(R == 8, "double-float butterflies of radix 2, 4, 8");
+            cdf e[4] = {v[0], v[2], v[4], v[6]};
+            cdf o[4] = {v[1], v[3], v[5], v[7]};
+            r4<FWD>(e);
+            r4<FWD>(o);
+            // o[k] *= w8^k; the products take renormalised operands
+            df const h(0.70710678118654752440);
+            cdf const o1 = o[1], o3 = o[3];
+            if (FWD){
+                o[1].x = h * norm(add(o1.x, o1.y)); o[1].y = h * norm(sub(o1.y, o1.x));
+                o[3].x = h * norm(sub(o3.y, o3.x)); o[3].y = -(h * norm(add(o3.x, o3.y)));
+            } else {
+                o[1].x = h * norm(sub(o1.x, o1.y)); o[1].y = h * norm(add(o1.y, o1.x));
+                o[3].x = -(h * norm(add(o3.x, o3.y))); o[3].y = h * norm(sub(o3.x, o3.y));
+            }
+            o[2] = rot<FWD>(o[2]);
+            for (int k = 0; k < 4; k++){ v[k] = cnorm(cadd(e[k], o[k])); v[k + 4] = cnorm(csub(e[k], o[k])); }
+        }
+    }
+};
+
 // multiply by -i (forward) or +i (backward)
 template<bool FWD, typename C> __device__ __forceinline__ C rot90(C a){
     C r;
@@ -317,7 +376,9 @@ __device__ __forceinline__ void bfly_prime(C *v){
 
 template<int R, bool FWD, typename C, typename T>
 __device__ __forceinline__ void bfly(C *v){
-    if constexpr (R == 1){
+    if constexpr (std::is_same<C, cdf>::value && (R == 2 || R == 4 || R == 8)){
+        dfb::bfly<R, FWD>(v);
+    } else if constexpr (R == 1){
         return;
     } else if constexpr (R == 2){
         C a = v[0], b = v[1];
