@@ -194,11 +194,28 @@ template<typename C> __device__ __forceinline__ C cmulc(C a, C b){
 }
 template<typename C> __device__ __forceinline__ C cconj(C a){ C r; r.x = a.x; r.y = -a.y; return r; }
 // double-float complex products through the fused dot (one renormalisation per part)
+// a * b + c * d without the final renormalisation: the rounded sum of the
+// head products and the sum of every lower-order term; the pair represents
+// the value as df_dot2's does, its tail not necessarily below half an ulp of
+// its head (the butterflies that take it renormalise)
+__host__ __device__ __forceinline__ df df_dot2_lazy(df a, df b, df c, df d){
+    float const p1 = mul_rn(a.hi, b.hi), p2 = mul_rn(c.hi, d.hi);
+    float const e1 = fmaf(a.hi, b.hi, -p1), e2 = fmaf(c.hi, d.hi, -p2);
+    float const s = p1 + p2;
+    float const bb = s - p1;
+    float e = ((p1 - (s - bb)) + (p2 - bb)) + (e1 + e2);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    e = fmaf(c.hi, d.lo, e);
+    e = fmaf(c.lo, d.hi, e);
+    return df(s, e);
+}
+// complex products of the twiddle multiplications (outputs not renormalised)
 __host__ __device__ __forceinline__ cdf cmul(cdf a, cdf b){
-    cdf r; r.x = df_dot2(a.x, b.x, -a.y, b.y); r.y = df_dot2(a.x, b.y, a.y, b.x); return r;
+    cdf r; r.x = df_dot2_lazy(a.x, b.x, -a.y, b.y); r.y = df_dot2_lazy(a.x, b.y, a.y, b.x); return r;
 }
 __host__ __device__ __forceinline__ cdf cmulc(cdf a, cdf b){
-    cdf r; r.x = df_dot2(a.x, b.x, a.y, b.y); r.y = df_dot2(a.y, b.x, -a.x, b.y); return r;
+    cdf r; r.x = df_dot2_lazy(a.x, b.x, a.y, b.y); r.y = df_dot2_lazy(a.y, b.x, -a.x, b.y); return r;
 }
 // Double-float butterflies of radix 2, 4 and 8 with one renormalisation per
 // output instead of one per addition: inside a butterfly the sums keep the
