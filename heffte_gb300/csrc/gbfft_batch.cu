@@ -277,8 +277,12 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         bool fwd = (v == &fu);
         // a unit waits only for units queued before it (no CTA can wait on a
         // tile that no CTA has claimed yet)
-        for (size_t j = 0; j < v->size(); j++)
+        for (size_t j = 0; j < v->size(); j++){
             if ((*v)[j].dep >= (int)j) throw Error(ST_INVALID, "internal error: batch unit queued before its dependency");
+            // the kernel runs r2c / c2r units as line tiles only (they are the x passes)
+            if (((*v)[j].kind == K_R2C || (*v)[j].kind == K_C2R) && (*v)[j].cols)
+                throw Error(ST_INVALID, "internal error: r2c batch unit along a strided dimension");
+        }
         for (auto const &U : *v){
             long long N = b->ffts[U.plan]->N;
             // forward: input (in_total) -> output (out_total); backward: input
