@@ -52,8 +52,8 @@ Batch::~Batch(){
     for (void *p : device_allocs) cudaFree(p);
 }
 
-static void const *batch_kernel(int prec, bool fwd, int values){
-    return values == 8 ? batch_kernel_e8(prec, fwd) : batch_kernel_e16(prec, fwd);
+static void const *batch_kernel(int prec, bool fwd, int values, bool r2c){
+    return values == 8 ? batch_kernel_e8(prec, fwd, r2c) : batch_kernel_e16(prec, fwd, r2c);
 }
 
 static int tile_tpb(Plan1D const &P, bool cols, size_t csize, size_t smem_cap, int tune_tpb){
@@ -279,9 +279,12 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         // tile that no CTA has claimed yet)
         for (size_t j = 0; j < v->size(); j++){
             if ((*v)[j].dep >= (int)j) throw Error(ST_INVALID, "internal error: batch unit queued before its dependency");
-            // the kernel runs r2c / c2r units as line tiles only (they are the x passes)
+            // the kernels run r2c / c2r units as line tiles only (they are the
+            // x passes), and those of r2c batches their c2c units as column tiles
             if (((*v)[j].kind == K_R2C || (*v)[j].kind == K_C2R) && (*v)[j].cols)
                 throw Error(ST_INVALID, "internal error: r2c batch unit along a strided dimension");
+            if (kind == PK_R2C && ((*v)[j].kind == K_C2C_F || (*v)[j].kind == K_C2C_B) && !(*v)[j].cols)
+                throw Error(ST_INVALID, "internal error: c2c unit of an r2c batch along x");
         }
         for (auto const &U : *v){
             long long N = b->ffts[U.plan]->N;
@@ -338,7 +341,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     if (b->pf_offset > 0) smem += (pf_bytes + 15) / 16 * 16;
     b->smem = smem;
     for (bool fwd : {true, false}){
-        void const *kern = batch_kernel(prec, fwd, values);
+        void const *kern = batch_kernel(prec, fwd, values, kind == PK_R2C);
         int nb_sm = 1;
         check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
         check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, kern, kBatchThreads, smem), "occupancy");
@@ -374,7 +377,7 @@ static void build_graph(Batch &b, bool fwd){
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
                     &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget, &b.pf_offset};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values));
+    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values, b.kind == PK_R2C));
     kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)b.smem;
@@ -471,7 +474,7 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
                     &args_total, &args_status, &args_scaling, &args_budget, &pf_offset};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values));
+    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values, kind == PK_R2C));
     kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)smem;

@@ -3,11 +3,17 @@
 
 namespace gbfft {
 
-void const *batch_kernel_e16(int prec, bool fwd){
-    if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 16>)
-                              : reinterpret_cast<void const*>(k_batch<float, false, 16>);
-    return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 16>)
-               : reinterpret_cast<void const*>(k_batch<double, false, 16>);
+void const *batch_kernel_e16(int prec, bool fwd, bool r2c){
+    if (r2c){
+        if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 16, true>)
+                                  : reinterpret_cast<void const*>(k_batch<float, false, 16, true>);
+        return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 16, true>)
+                   : reinterpret_cast<void const*>(k_batch<double, false, 16, true>);
+    }
+    if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 16, false>)
+                              : reinterpret_cast<void const*>(k_batch<float, false, 16, false>);
+    return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 16, false>)
+               : reinterpret_cast<void const*>(k_batch<double, false, 16, false>);
 }
 
 } // namespace gbfft

@@ -102,7 +102,10 @@ template<class F> struct PrefetchHook {
     __device__ __forceinline__ void operator()() const { f(); }
 };
 
-template<typename T, bool FWD, int EMAX>
+// R2C: the kernel of r2c batches, whose r2c / c2r units are x passes (line
+// tiles) and whose c2c units are y / z passes (column tiles): it compiles
+// those paths alone (fewer registers and less spill code)
+template<typename T, bool FWD, int EMAX, bool R2C>
 __global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
@@ -238,14 +241,15 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 // then spills less, 1.44 against 1.61 ms per step of 256
                 // boxes; the 16-value kernel keeps both paths, which measured
                 // faster for it, 1.41 against 1.48 ms)
-                if constexpr (EMAX == 8)
+                if constexpr (EMAX == 8 || R2C)
                     tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
                 else if (U.cols) tile_r2c<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
                 else tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                if constexpr (R2C) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                else if (U.cols) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
                 else tile_c2c<T, EMAX, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
             }
         } else {
@@ -253,14 +257,15 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 T *out = reinterpret_cast<T*>(dstb) + U.out_off;
                 // the c2r pass runs along x: line tiles (as for r2c above)
-                if constexpr (EMAX == 8)
+                if constexpr (EMAX == 8 || R2C)
                     tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
                 else if (U.cols) tile_c2r<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
                 else tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if (U.cols) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                if constexpr (R2C) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                else if (U.cols) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
                 else tile_c2c<T, EMAX, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
             }
         }
@@ -273,9 +278,9 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
     }
 }
 
-// k_batch<T, FWD, EMAX> for EMAX = 16 (any radix plan, radices up to 16) and
-// EMAX = 8 (radices up to 8: fewer registers per thread); cast to a pointer
-void const *batch_kernel_e16(int prec, bool fwd);
-void const *batch_kernel_e8(int prec, bool fwd);
+// k_batch<T, FWD, EMAX, R2C> for EMAX = 16 (any radix plan, radices up to 16)
+// and EMAX = 8 (radices up to 8: fewer registers per thread); cast to a pointer
+void const *batch_kernel_e16(int prec, bool fwd, bool r2c);
+void const *batch_kernel_e8(int prec, bool fwd, bool r2c);
 
 } // namespace gbfft
