@@ -52,8 +52,8 @@ Batch::~Batch(){
     for (void *p : device_allocs) cudaFree(p);
 }
 
-static void const *batch_kernel(int prec, bool fwd, int values, bool r2c){
-    return values == 8 ? batch_kernel_e8(prec, fwd, r2c) : batch_kernel_e16(prec, fwd, r2c);
+static void const *batch_kernel(int prec, bool fwd, int values, bool r2c, bool s5){
+    return values == 8 ? batch_kernel_e8(prec, fwd, r2c, s5) : batch_kernel_e16(prec, fwd, r2c, s5);
 }
 
 static int tile_tpb(Plan1D const &P, bool cols, size_t csize, size_t smem_cap, int tune_tpb){
@@ -166,6 +166,15 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
         b->ffts.push_back(f);
         tpb_hint.push_back(hint);
     }
+    // every plan 5-smooth (radices 2, 3, 4, 5, 8, 16): the kernels without
+    // the radix-7/11/13 stages
+    bool s5 = true;
+    for (auto const &P : plans)
+        for (int st = 0; st < P.nstages; st++){
+            int const R = P.st[st].R;
+            s5 = s5 && (R == 2 || R == 3 || R == 4 || R == 5 || R == 8 || R == 16);
+        }
+    b->s5 = s5;
     size_t smem_cap = (size_t)config.tile_kb * 1024;
     // units: forward = (r2c|c2c x), c2c y, c2c z; backward = c2c z, c2c y, (c2r|c2c x)
     auto build = [&](bool fwd, std::vector<BatchUnit> &units, long long &total){
@@ -341,7 +350,7 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     if (b->pf_offset > 0) smem += (pf_bytes + 15) / 16 * 16;
     b->smem = smem;
     for (bool fwd : {true, false}){
-        void const *kern = batch_kernel(prec, fwd, values, kind == PK_R2C);
+        void const *kern = batch_kernel(prec, fwd, values, kind == PK_R2C, s5);
         int nb_sm = 1;
         check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
         check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, kern, kBatchThreads, smem), "occupancy");
@@ -377,7 +386,7 @@ static void build_graph(Batch &b, bool fwd){
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
                     &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget, &b.pf_offset};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values, b.kind == PK_R2C));
+    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values, b.kind == PK_R2C, b.s5));
     kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)b.smem;
@@ -474,7 +483,7 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
                     &args_total, &args_status, &args_scaling, &args_budget, &pf_offset};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values, kind == PK_R2C));
+    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values, kind == PK_R2C, s5));
     kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)smem;

@@ -3,17 +3,24 @@
 
 namespace gbfft {
 
-void const *batch_kernel_e8(int prec, bool fwd, bool r2c){
-    if (r2c){
-        if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 8, true>)
-                                  : reinterpret_cast<void const*>(k_batch<float, false, 8, true>);
-        return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 8, true>)
-                   : reinterpret_cast<void const*>(k_batch<double, false, 8, true>);
+void const *batch_kernel_e8(int prec, bool fwd, bool r2c, bool s5){
+    // r2c batches: 5-smooth or any plans; other batches: any plans
+    if (r2c && s5){
+        if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 8, true, true>)
+                                  : reinterpret_cast<void const*>(k_batch<float, false, 8, true, true>);
+        return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 8, true, true>)
+                   : reinterpret_cast<void const*>(k_batch<double, false, 8, true, true>);
     }
-    if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 8, false>)
-                              : reinterpret_cast<void const*>(k_batch<float, false, 8, false>);
-    return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 8, false>)
-               : reinterpret_cast<void const*>(k_batch<double, false, 8, false>);
+    if (r2c){
+        if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 8, true, false>)
+                                  : reinterpret_cast<void const*>(k_batch<float, false, 8, true, false>);
+        return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 8, true, false>)
+                   : reinterpret_cast<void const*>(k_batch<double, false, 8, true, false>);
+    }
+    if (prec == 0) return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 8, false, false>)
+                              : reinterpret_cast<void const*>(k_batch<float, false, 8, false, false>);
+    return fwd ? reinterpret_cast<void const*>(k_batch<double, true, 8, false, false>)
+               : reinterpret_cast<void const*>(k_batch<double, false, 8, false, false>);
 }
 
 } // namespace gbfft

@@ -105,7 +105,9 @@ template<class F> struct PrefetchHook {
 // R2C: the kernel of r2c batches, whose r2c / c2r units are x passes (line
 // tiles) and whose c2c units are y / z passes (column tiles): it compiles
 // those paths alone (fewer registers and less spill code)
-template<typename T, bool FWD, int EMAX, bool R2C>
+// S5: every radix plan of the batch is 5-smooth (radices 2, 3, 4, 5, 8, 16):
+// the stages of radix 7, 11 and 13 are not compiled (fewer registers)
+template<typename T, bool FWD, int EMAX, bool R2C, bool S5>
 __global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
@@ -242,15 +244,15 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 // boxes; the 16-value kernel keeps both paths, which measured
                 // faster for it, 1.41 against 1.48 ms)
                 if constexpr (EMAX == 8 || R2C)
-                    tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
-                else if (U.cols) tile_r2c<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
-                else tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook);
+                    tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, std::integral_constant<bool, S5>{});
+                else if (U.cols) tile_r2c<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, std::integral_constant<bool, S5>{});
+                else tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, std::integral_constant<bool, S5>{});
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if constexpr (R2C) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else if (U.cols) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else tile_c2c<T, EMAX, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                if constexpr (R2C) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                else if (U.cols) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                else tile_c2c<T, EMAX, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
             }
         } else {
             if (U.kind == K_C2R){
@@ -258,15 +260,15 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 T *out = reinterpret_cast<T*>(dstb) + U.out_off;
                 // the c2r pass runs along x: line tiles (as for r2c above)
                 if constexpr (EMAX == 8 || R2C)
-                    tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else if (U.cols) tile_c2r<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                    tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                else if (U.cols) tile_c2r<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                else tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if constexpr (R2C) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else if (U.cols) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
-                else tile_c2c<T, EMAX, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook);
+                if constexpr (R2C) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                else if (U.cols) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                else tile_c2c<T, EMAX, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
             }
         }
         // publish completion of this tile
@@ -280,7 +282,7 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
 
 // k_batch<T, FWD, EMAX, R2C> for EMAX = 16 (any radix plan, radices up to 16)
 // and EMAX = 8 (radices up to 8: fewer registers per thread); cast to a pointer
-void const *batch_kernel_e16(int prec, bool fwd, bool r2c);
-void const *batch_kernel_e8(int prec, bool fwd, bool r2c);
+void const *batch_kernel_e16(int prec, bool fwd, bool r2c, bool s5);
+void const *batch_kernel_e8(int prec, bool fwd, bool r2c, bool s5);
 
 } // namespace gbfft

@@ -90,10 +90,13 @@ struct NoHook {
 
 // Runs the whole transform. If last_to_global is false the result is left in
 // shared memory (natural order) and the CTA is synchronised on return.
-template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST, class AF = NoHook>
+// S5T: std::true_type compiles the radices of 5-smooth lengths alone (2, 3,
+// 4, 5, 8, 16; the caller guarantees the plan has no other): fewer registers
+template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST, class AF = NoHook, class S5T = std::false_type>
 __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
                                         c_t<T> const *__restrict__ tw, bool last_to_global, LD &ld, ST &st,
-                                        AF const &after_first = AF{}){
+                                        AF const &after_first = AF{}, S5T = S5T{}){
+    constexpr bool S5 = S5T::value;
     constexpr bool HOOK = !std::is_same<AF, NoHook>::value;
     Regs<T, EMAX> r;
     if (P.nstages == 0){
@@ -114,10 +117,10 @@ __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t
         bool tg = (s == P.nstages - 1) && last_to_global;
         switch (S.R){
             case 16: if constexpr (EMAX >= 16) fft_stage<16, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 13: if constexpr (EMAX >= 13) fft_stage<13, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 11: if constexpr (EMAX >= 11) fft_stage<11, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 13: if constexpr (EMAX >= 13 && !S5) fft_stage<13, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 11: if constexpr (EMAX >= 11 && !S5) fft_stage<11, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
             case 8: fft_stage<8, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 7: fft_stage<7, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 7: if constexpr (!S5) fft_stage<7, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
             case 5: fft_stage<5, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
             case 4: fft_stage<4, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
             case 3: fft_stage<3, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
@@ -152,11 +155,11 @@ __device__ __forceinline__ int padded_len(int N){ return N + (N >> 4) + 1; }
 // pf (optional): the tile's input already copied into shared memory, lines
 // back to back (pf[loc * N + p]) or rows of TPB columns (pf[p * TPB + loc]);
 // after_first: see fft_run.
-template<typename T, int EMAX, bool FWD, bool COLS, class AF = NoHook>
+template<typename T, int EMAX, bool FWD, bool COLS, class AF = NoHook, class S5T = std::false_type>
 __device__ __forceinline__ void tile_c2c(Plan1D const &P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out,
                                          c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
                                          long long tile, c_t<T> *sm, c_t<T> const *pf = nullptr,
-                                         AF const &after_first = AF{}){
+                                         AF const &after_first = AF{}, S5T s5 = S5T{}){
     using C = c_t<T>;
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
@@ -172,7 +175,7 @@ __device__ __forceinline__ void tile_c2c(Plan1D const &P, Layout Li, Layout Lo, 
         return __ldcg(in + ib + p * ies);
     };
     auto st = [&](int p, C v){ out[ob + p * oes] = do_scale ? cscale(v, scale) : v; };
-    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st, after_first);
+    fft_run<EMAX, FWD, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st, after_first, s5);
 }
 
 template<typename T, int EMAX, bool FWD, bool COLS>
@@ -191,11 +194,11 @@ k_c2c(Plan1D P, Layout Li, Layout Lo, c_t<T> const *in, c_t<T> *out, c_t<T> cons
 // ---------------------------------------------------------------------------
 // pf (optional, line tiles): the tile's real input lines back to back in
 // shared memory (line 2 loc + b at pf[(2 loc + b) N + p])
-template<typename T, int EMAX, bool COLS, class AF = NoHook>
+template<typename T, int EMAX, bool COLS, class AF = NoHook, class S5T = std::false_type>
 __device__ __forceinline__ void tile_r2c(Plan1D const &P, Layout Li, Layout Lo, T const *in, c_t<T> *out,
                                          c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
                                          long long tile, c_t<T> *sm, T const *pf = nullptr,
-                                         AF const &after_first = AF{}){
+                                         AF const &after_first = AF{}, S5T s5 = S5T{}){
     using C = c_t<T>;
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
@@ -216,7 +219,7 @@ __device__ __forceinline__ void tile_r2c(Plan1D const &P, Layout Li, Layout Lo, 
     };
     auto st = [&](int, C){};
     int padn = padded_len(P.N);
-    fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, false, ld, st, after_first);
+    fft_run<EMAX, true, COLS, T>(P, t, active, sm, loc, TPB, padn, tw, false, ld, st, after_first, s5);
     if (!active) return;
     int N = P.N;
     long long oa = base_of(Lo, ga), obb = hasb ? base_of(Lo, gb) : 0;
@@ -252,11 +255,11 @@ k_r2c(Plan1D P, Layout Li, Layout Lo, T const *in, c_t<T> *out, c_t<T> const *__
 // ---------------------------------------------------------------------------
 // pf (optional, line tiles): the tile's half-spectrum lines back to back in
 // shared memory (line 2 loc + b at pf[(2 loc + b) (N/2 + 1) + p])
-template<typename T, int EMAX, bool COLS, class AF = NoHook>
+template<typename T, int EMAX, bool COLS, class AF = NoHook, class S5T = std::false_type>
 __device__ __forceinline__ void tile_c2r(Plan1D const &P, Layout Li, Layout Lo, c_t<T> const *in, T *out,
                                          c_t<T> const *__restrict__ tw, long long G, int TPB, T scale, int do_scale,
                                          long long tile, c_t<T> *sm, c_t<T> const *pf = nullptr,
-                                         AF const &after_first = AF{}){
+                                         AF const &after_first = AF{}, S5T s5 = S5T{}){
     using C = c_t<T>;
     int loc, t;
     thread_map<COLS>(TPB, P.T, loc, t);
@@ -290,7 +293,7 @@ __device__ __forceinline__ void tile_c2r(Plan1D const &P, Layout Li, Layout Lo, 
         out[oa + p * oes] = v.x * s;
         if (hasb) out[obb + p * oes] = v.y * s;
     };
-    fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st, after_first);
+    fft_run<EMAX, false, COLS, T>(P, t, active, sm, loc, TPB, padded_len(P.N), tw, true, ld, st, after_first, s5);
 }
 
 template<typename T, int EMAX, bool COLS>

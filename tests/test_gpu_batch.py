@@ -188,3 +188,30 @@ def test_batch_autotune_keeps_a_correct_shape(gb):
         xi = x[b.input_offset(i):b.input_offset(i) + m]
         yi = yh[b.output_offset(i):b.output_offset(i) + m]
         assert O.rel_l2(yi, O.fft3d_c2c(xi, s)) < TOL[0], (i, s)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_r2c_batch_with_sides_of_prime_factors_7_11_13(gb, prec):
+    """Sides with factors 7, 11 and 13 (the kernels with every radix stage)
+    beside 5-smooth ones (the kernels without the radix-7/11/13 stages run
+    only batches whose plans are all 5-smooth), forward and round trip."""
+    rng = np.random.default_rng(77 + prec)
+    sizes = _sizes(rng, 12, [56, 44, 52, 28, 112, 16, 40])
+    b = gb.boxbatch(gb.kind.r2c, sizes, prec)
+    rdt, cdt = (np.float32, torch.complex64) if prec == 0 else (np.float64, torch.complex128)
+    x = rng.standard_normal(b.input_size()).astype(rdt)
+    xin = torch.from_numpy(x).cuda()
+    y = torch.empty(b.output_size(), dtype=cdt, device="cuda")
+    b.forward(xin, y)
+    yh = y.cpu().numpy()
+    for i, s in enumerate(sizes):
+        n = int(np.prod(s))
+        nc = (s[0] // 2 + 1) * s[1] * s[2]
+        xi = x[b.input_offset(i):b.input_offset(i) + n]
+        yi = yh[b.output_offset(i):b.output_offset(i) + nc]
+        assert O.rel_l2(yi, O.fft3d_r2c(xi, s, 0)) < TOL[prec], (i, s)
+    w = torch.empty(b.workspace_size(), dtype=cdt, device="cuda")
+    z = torch.empty_like(xin)
+    b.backward(y, z, w, gb.scale.full)
+    assert O.rel_l2(z.cpu().numpy(), x) < 3 * TOL[prec]
+    assert gb.device_status() == 0
