@@ -84,7 +84,12 @@ __device__ __forceinline__ void cp_async_cg16(void *dst, void const *src){
 
 // CTAs per SM the batch kernels are compiled for (registers per thread
 // <= 65536 / (256 x this)); float measured best at 4, double kept at 2
-template<typename T> constexpr int batch_ctas_per_sm(){ return sizeof(T) == 4 ? 4 : 2; }
+template<typename T, int EMAX = 16, bool R2C = false> constexpr int batch_ctas_per_sm(){
+    // the float kernel of r2c batches with 16 values per thread: three CTAs
+    // (80 registers, about 1 KB of spill code) beat four (64 registers, 3 KB):
+    // 1.15 against 1.22 ms per step of 256 boxes (five: 1.42-1.51)
+    return sizeof(T) == 4 ? ((R2C && EMAX == 16) ? 3 : 4) : 2;
+}
 
 // scaling: 0 none, 1 full (1/N of each box), 2 symmetric.  One kernel per
 // direction: the forward one holds the r2c and forward c2c tile paths, the
@@ -108,7 +113,7 @@ template<class F> struct PrefetchHook {
 // S5: every radix plan of the batch is 5-smooth (radices 2, 3, 4, 5, 8, 16):
 // the stages of radix 7, 11 and 13 are not compiled (fewer registers)
 template<typename T, bool FWD, int EMAX, bool R2C, bool S5>
-__global__ void __launch_bounds__(256, batch_ctas_per_sm<T>())
+__global__ void __launch_bounds__(256, batch_ctas_per_sm<T, EMAX, R2C>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
         long long total_tiles, int *status, int scaling, long long dep_budget, int pf_offset){
