@@ -53,7 +53,9 @@ Batch::~Batch(){
 }
 
 static void const *batch_kernel(int prec, bool fwd, int values, bool r2c, bool s5){
-    return values == 8 ? batch_kernel_e8(prec, fwd, r2c, s5) : batch_kernel_e16(prec, fwd, r2c, s5);
+    if (values == 8) return batch_kernel_e8(prec, fwd, r2c, s5);
+    if (r2c) return s5 ? batch_kernel_e16_r2c5(prec, fwd) : batch_kernel_e16_r2c(prec, fwd);
+    return batch_kernel_e16_any(prec, fwd);
 }
 
 static int tile_tpb(Plan1D const &P, bool cols, size_t csize, size_t smem_cap, int tune_tpb){

@@ -287,7 +287,9 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
 
 // k_batch<T, FWD, EMAX, R2C> for EMAX = 16 (any radix plan, radices up to 16)
 // and EMAX = 8 (radices up to 8: fewer registers per thread); cast to a pointer
-void const *batch_kernel_e16(int prec, bool fwd, bool r2c, bool s5);
+void const *batch_kernel_e16_any(int prec, bool fwd);
+void const *batch_kernel_e16_r2c(int prec, bool fwd);
+void const *batch_kernel_e16_r2c5(int prec, bool fwd);
 void const *batch_kernel_e8(int prec, bool fwd, bool r2c, bool s5);
 
 } // namespace gbfft
