@@ -154,6 +154,9 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
     }
     __syncthreads();
     while (true){
+        // thread 0 takes the claimed tile, claims the next one and waits for
+        // the taken tile's pass dependency; one barrier hands all of it to the CTA
+        bool ok = true;
         if (tid == 0){
             s_tile = s_next;
             s_unit = s_next_unit;
@@ -163,28 +166,27 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 long long nx = (long long)atomicAdd(work_counter, 1ull);
                 s_next = nx;
                 s_next_unit = (nx < total_tiles) ? find_unit(nx) : 0;
+                BatchUnit const &W = units[s_unit];
+                // a prefetched tile's dependency was met before its copy was issued
+                if (W.dep >= 0 && !s_pf_cur){
+                    long long need = units[W.dep].tiles + W.dep_extra;
+                    volatile int *d = done + W.dep;
+                    if (*d < need){
+                        long long t0 = clock64();
+                        while (*d < need){
+                            if (clock64() - t0 > dep_budget){ atomicExch(status, DEV_TIMEOUT_DEPENDENCY); ok = false; break; }
+                        }
+                    }
+                    __threadfence();
+                }
             }
         }
-        __syncthreads();
+        if (__syncthreads_or(!ok)) return;
         long long gt = s_tile;
         int u = s_unit;
         bool const pfcur = s_pf_cur != 0;
         if (gt >= total_tiles) return;
         BatchUnit const &U = units[u];
-        bool ok = true;
-        // a prefetched tile's dependency was met before its copy was issued
-        if (tid == 0 && U.dep >= 0 && !pfcur){
-            long long need = units[U.dep].tiles + U.dep_extra;
-            volatile int *d = done + U.dep;
-            if (*d < need){
-                long long t0 = clock64();
-                while (*d < need){
-                    if (clock64() - t0 > dep_budget){ atomicExch(status, DEV_TIMEOUT_DEPENDENCY); ok = false; break; }
-                }
-            }
-            __threadfence();
-        }
-        if (__syncthreads_or(!ok)) return;
         if (pfcur){
             asm volatile("cp.async.wait_all;" ::: "memory");
             __syncthreads();
