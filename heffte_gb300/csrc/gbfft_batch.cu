@@ -296,6 +296,8 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
                 throw Error(ST_INVALID, "internal error: r2c batch unit along a strided dimension");
             if (kind == PK_R2C && ((*v)[j].kind == K_C2C_F || (*v)[j].kind == K_C2C_B) && !(*v)[j].cols)
                 throw Error(ST_INVALID, "internal error: c2c unit of an r2c batch along x");
+            if (kind == PK_C2C && ((*v)[j].kind == K_R2C || (*v)[j].kind == K_C2R))
+                throw Error(ST_INVALID, "internal error: r2c unit in a c2c batch");
         }
         for (auto const &U : *v){
             long long N = b->ffts[U.plan]->N;

@@ -85,10 +85,10 @@ __device__ __forceinline__ void cp_async_cg16(void *dst, void const *src){
 // CTAs per SM the batch kernels are compiled for (registers per thread
 // <= 65536 / (256 x this)); float measured best at 4, double kept at 2
 template<typename T, int EMAX = 16, bool R2C = false> constexpr int batch_ctas_per_sm(){
-    // the float kernel of r2c batches with 16 values per thread: three CTAs
-    // (80 registers, about 1 KB of spill code) beat four (64 registers, 3 KB):
-    // 1.15 against 1.22 ms per step of 256 boxes (five: 1.42-1.51)
-    return sizeof(T) == 4 ? ((R2C && EMAX == 16) ? 3 : 4) : 2;
+    // the float kernels with 16 values per thread: three CTAs (80 registers,
+    // about 1 KB of spill code) beat four (64 registers, 3 KB): 1.15 against
+    // 1.22 ms per step of 256 r2c boxes (five: 1.42-1.51)
+    return sizeof(T) == 4 ? ((EMAX == 16) ? 3 : 4) : 2;
 }
 
 // scaling: 0 none, 1 full (1/N of each box), 2 symmetric.  One kernel per
@@ -109,7 +109,8 @@ template<class F> struct PrefetchHook {
 
 // R2C: the kernel of r2c batches, whose r2c / c2r units are x passes (line
 // tiles) and whose c2c units are y / z passes (column tiles): it compiles
-// those paths alone (fewer registers and less spill code)
+// those paths alone (fewer registers and less spill code); without it, the
+// kernel of c2c batches (c2c line and column tiles)
 // S5: every radix plan of the batch is 5-smooth (radices 2, 3, 4, 5, 8, 16):
 // the stages of radix 7, 11 and 13 are not compiled (fewer registers)
 template<typename T, bool FWD, int EMAX, bool R2C, bool S5>
@@ -241,7 +242,8 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
         int dsc = U.last && scaling != 0;
         C const *pfc = pfcur ? reinterpret_cast<C const*>(pfbuf) : nullptr;
         if constexpr (FWD){
-            if (U.kind == K_R2C){
+            // (R2C false: the kernel of c2c batches, which have no r2c unit)
+            if (R2C && U.kind == K_R2C){
                 T const *in = reinterpret_cast<T const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
                 T const *pfr = pfcur ? reinterpret_cast<T const*>(pfbuf) : nullptr;
@@ -262,7 +264,7 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 else tile_c2c<T, EMAX, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
             }
         } else {
-            if (U.kind == K_C2R){
+            if (R2C && U.kind == K_C2R){
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 T *out = reinterpret_cast<T*>(dstb) + U.out_off;
                 // the c2r pass runs along x: line tiles (as for r2c above)
