@@ -86,8 +86,9 @@ __device__ __forceinline__ void cp_async_cg16(void *dst, void const *src){
 // <= 65536 / (256 x this)); float measured best at 4, double kept at 2
 template<typename T, int EMAX = 16, bool R2C = false> constexpr int batch_ctas_per_sm(){
     // the float kernels with 16 values per thread: three CTAs (80 registers,
-    // about 1 KB of spill code) beat four (64 registers, 3 KB): 1.15 against
-    // 1.22 ms per step of 256 r2c boxes (five: 1.42-1.51)
+    // about 1 KB of spill code) beat four (64 registers, 3-5 KB): 1.15
+    // against 1.22 ms per step of 256 r2c boxes (five: 1.42-1.51), 1.87
+    // against 2.19 ms for the same boxes as c2c
     return sizeof(T) == 4 ? ((EMAX == 16) ? 3 : 4) : 2;
 }
 
