@@ -24,3 +24,22 @@ def test_double_float_arithmetic_on_the_host(tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout
     assert r.stdout.count(" ok") == 12
+
+
+def test_pipelined_plans_and_swizzle_on_the_host(tmp_path):
+    """The compile-time tables of the pipelined kernels (heffte_gb300/csrc/
+    gbfft_pipe.cuh) evaluated on the host: radix plans multiply to their
+    lengths (double-float plans with radices up to 8 and 8 values per
+    thread), twiddle offsets in the Stockham layout, and the swizzle of the
+    double-float line exchange a conflict-free permutation for every stage."""
+    nvcc = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
+    if nvcc is None:
+        pytest.skip("nvcc not found")
+    root = os.path.dirname(HERE)
+    exe = str(tmp_path / "check_plans")
+    subprocess.run([nvcc, "-O1", "-std=c++17", "--expt-relaxed-constexpr", "-I" + os.path.join(root, "include"),
+                    "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe,
+                    os.path.join(HERE, "df_host", "check_plans.cu")],
+                   check=True, capture_output=True, cwd=str(tmp_path), timeout=600)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "plans and swizzle ok" in r.stdout, r.stdout
