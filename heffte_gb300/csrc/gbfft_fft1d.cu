@@ -432,6 +432,9 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
     return launch_pipe_f64_r2r(s, kind, f.N, cols, a);
 }
 
+#ifndef GBFFT_RT_SLOTS
+#define GBFFT_RT_SLOTS 1
+#endif
 // Pipelined runtime-radix path (c2c of any supported length): line tiles need
 // back-to-back lines whose tile bytes are multiples of 16, column tiles a
 // tensor map over adjacent columns.  Returns false when the batch does not
@@ -455,12 +458,15 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     std::memset(&tmap, 0, sizeof(tmap));
     int tpb;
     size_t smem;
+    // tile slots: one for float (the kernel is compiled for two CTAs per SM,
+    // which overlap each other's copies), two for double
+    int const nbuf = (prec == 0) ? GBFFT_RT_SLOTS : 2;
     if (!cols){
         if (Li.dist != N || (G > Li.count && Li.bstride != Li.count * N)) return false;
         tpb = std::max(1, 256 / T);
         while (tpb > 1 && tpb * T > 512) tpb /= 2;
-        while (tpb > 1 && (2 * (size_t)tpb * N + (size_t)tpb * padn) * es > 200 * 1024) tpb /= 2;
-        smem = (2 * (size_t)tpb * N + (size_t)tpb * padn) * es;
+        while (tpb > 1 && (nbuf * (size_t)tpb * N + (size_t)tpb * padn) * es > 200 * 1024) tpb /= 2;
+        smem = (nbuf * (size_t)tpb * N + (size_t)tpb * padn) * es;
         long long last = G % tpb;
         if (((size_t)tpb * N * es) % 16 != 0 || ((size_t)last * N * es) % 16 != 0) return false;
         P.ntiles = (G + tpb - 1) / tpb;
@@ -469,9 +475,9 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
         if (Li.dist != 1 || G % Li.count != 0) return false;
         tpb = (prec == 0) ? 16 : 8;
         while (tpb > 2 && tpb * T > 512) tpb /= 2;
-        while (tpb > 2 && 2 * (size_t)tpb * N * es > 200 * 1024) tpb /= 2;
+        while (tpb > 2 && nbuf * (size_t)tpb * N * es > 200 * 1024) tpb /= 2;
         if (((size_t)tpb * es) % 16 != 0 || tpb * T > 512) return false;
-        smem = 2 * (size_t)tpb * N * es;
+        smem = nbuf * (size_t)tpb * N * es;
         // the rows of each tensor copy: a divisor of N up to 256 whose box
         // (and so every box destination) is a multiple of 128 bytes, as is
         // the tile buffer, since a tensor copy's shared-memory destination
@@ -495,6 +501,7 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     P.tw = f.twiddles(prec, s);
     P.G = G;
     P.tpb = tpb;
+    P.nbuf = nbuf;
     P.scale = scale;
     P.do_scale = (scale != 1.0);
     P.status = device_status();

@@ -190,6 +190,7 @@ struct PipeRtParams {
     long long ntiles;
     long long tiles_per_block;   // column tiles covering one block of `count` columns
     int tpb;                     // transforms per tile
+    int nbuf;                    // tile slots: 2 (the next tile copied while one is transformed) or 1
     int boxr;                    // rows per tensor-map copy (divides N)
     int tswap;
     double scale;

@@ -47,8 +47,10 @@ __device__ __forceinline__ void rt_stages(Plan1D const &P, int t, bool active, c
     }
 }
 
+// float: compiled for two 512-thread CTAs per SM (64 registers, no spills):
+// with one tile slot the CTAs on an SM overlap each other's copies
 template<typename T, bool FWD, bool COLS, int LOADER>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
 k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
     constexpr int EMAX = kEmax;
@@ -58,7 +60,8 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
     int const padn = padded_len(N);
     long long const TILE = (long long)TPB * N;             // complex values per tile buffer
     C *tiles = reinterpret_cast<C*>(smraw);
-    C *xline = tiles + 2 * TILE;                           // line tiles: padded exchange buffer
+    int const nbuf = P.nbuf;
+    C *xline = tiles + nbuf * TILE;                        // line tiles: padded exchange buffer
     int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     int loc, t;
     thread_map<COLS>(TPB, P.plan.T, loc, t);
@@ -100,15 +103,21 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
 
     uint32_t ph0 = 0, ph1 = 0;
     long long tile = blockIdx.x;
-    if (tile < P.ntiles) issue(tile, 0);
+    if (nbuf == 2 && tile < P.ntiles) issue(tile, 0);
     T const sc = (T)P.scale;
     C const *tw = reinterpret_cast<C const*>(P.tw);
     for (int it = 0; tile < P.ntiles; tile += gridDim.x, it++){
-        int b = it & 1;
-        long long nxt = tile + gridDim.x;
-        if (nxt < P.ntiles){
+        int b = (nbuf == 2) ? (it & 1) : 0;
+        if (nbuf == 2){
+            long long nxt = tile + gridDim.x;
+            if (nxt < P.ntiles){
+                if (warp == 0) fence_proxy_async_smem();
+                issue(nxt, b ^ 1);
+            }
+        } else {
+            // one slot: this tile's copy, after the last iteration's barrier
             if (warp == 0) fence_proxy_async_smem();
-            issue(nxt, b ^ 1);
+            issue(tile, 0);
         }
         bool ok = mbar_wait_bounded(&bar[b], b ? ph1 : ph0, P.status);
         if (__syncthreads_or(!ok)) return;
