@@ -432,9 +432,16 @@ static bool try_pipe(cudaStream_t s, int kind, Fft1D &f, int prec, Layout Li, La
     return launch_pipe_f64_r2r(s, kind, f.N, cols, a);
 }
 
-#ifndef GBFFT_RT_SLOTS
-#define GBFFT_RT_SLOTS 1
-#endif
+// Whether two CTAs of `smem` dynamic shared-memory bytes are resident on
+// one SM of the current device (with the per-block reservation).
+static bool two_ctas_fit(size_t smem){
+    int dev = 0, smem_sm = 0, smem_rsv = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    check_cuda(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev), "device attribute");
+    check_cuda(cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev), "device attribute");
+    return 2 * (smem + (size_t)smem_rsv) <= (size_t)smem_sm;
+}
+
 // Pipelined runtime-radix path (c2c of any supported length): line tiles need
 // back-to-back lines whose tile bytes are multiples of 16, column tiles a
 // tensor map over adjacent columns.  Returns false when the batch does not
@@ -456,28 +463,40 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     PipeRtParams P{};
     CUtensorMap tmap;
     std::memset(&tmap, 0, sizeof(tmap));
-    int tpb;
-    size_t smem;
-    // tile slots: one for float (the kernel is compiled for two CTAs per SM,
-    // which overlap each other's copies), two for double
-    int const nbuf = (prec == 0) ? GBFFT_RT_SLOTS : 2;
+    int tpb = 1;
+    size_t smem = 0;
+    // tile slots: two (the copy of the next tile overlaps the transform of
+    // this one), or, for float when two CTAs of two slots do not fit in an
+    // SM's shared memory, one (the float kernel is compiled for two CTAs per
+    // SM, which then overlap each other's copies)
+    int nbuf = 2;
+    auto shape = [&](int nb){
+        if (!cols){
+            tpb = std::max(1, 256 / T);
+            while (tpb > 1 && tpb * T > 512) tpb /= 2;
+            while (tpb > 1 && (nb * (size_t)tpb * N + (size_t)tpb * padn) * es > 200 * 1024) tpb /= 2;
+            smem = (nb * (size_t)tpb * N + (size_t)tpb * padn) * es;
+        } else {
+            tpb = (prec == 0) ? 16 : 8;
+            while (tpb > 2 && tpb * T > 512) tpb /= 2;
+            while (tpb > 2 && nb * (size_t)tpb * N * es > 200 * 1024) tpb /= 2;
+            smem = nb * (size_t)tpb * N * es;
+        }
+    };
+    shape(nbuf);
+    if (prec == 0 && !two_ctas_fit(smem)){
+        nbuf = 1;
+        shape(nbuf);
+    }
     if (!cols){
         if (Li.dist != N || (G > Li.count && Li.bstride != Li.count * N)) return false;
-        tpb = std::max(1, 256 / T);
-        while (tpb > 1 && tpb * T > 512) tpb /= 2;
-        while (tpb > 1 && (nbuf * (size_t)tpb * N + (size_t)tpb * padn) * es > 200 * 1024) tpb /= 2;
-        smem = (nbuf * (size_t)tpb * N + (size_t)tpb * padn) * es;
         long long last = G % tpb;
         if (((size_t)tpb * N * es) % 16 != 0 || ((size_t)last * N * es) % 16 != 0) return false;
         P.ntiles = (G + tpb - 1) / tpb;
         P.tiles_per_block = 0;
     } else {
         if (Li.dist != 1 || G % Li.count != 0) return false;
-        tpb = (prec == 0) ? 16 : 8;
-        while (tpb > 2 && tpb * T > 512) tpb /= 2;
-        while (tpb > 2 && nbuf * (size_t)tpb * N * es > 200 * 1024) tpb /= 2;
         if (((size_t)tpb * es) % 16 != 0 || tpb * T > 512) return false;
-        smem = nbuf * (size_t)tpb * N * es;
         // the rows of each tensor copy: a divisor of N up to 256 whose box
         // (and so every box destination) is a multiple of 128 bytes, as is
         // the tile buffer, since a tensor copy's shared-memory destination

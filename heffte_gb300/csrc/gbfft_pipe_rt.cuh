@@ -1,5 +1,5 @@
 // Pipelined complex transforms of any supported length (runtime radix plan):
-// the persistent, double-buffered tile pipeline of the power-of-two kernels
+// the persistent tile pipeline of the power-of-two kernels
 // (lines by 1-D bulk copies, columns by 3-D tensor-map copies, both
 // completing on mbarriers with bounded waits) around the runtime Stockham
 // stages of the generic kernels (radices 2, 3, 4, 5, 7, 8, 11, 13, 16).
@@ -10,7 +10,9 @@
 //   * column tiles: TPB adjacent columns land as a [row][column] tile, which
 //     is the stages' exchange layout, so every stage (stage 0 included) runs
 //     in place in the tile.
-// While a tile is transformed the next one is already being copied in.
+// With two tile slots the next tile is copied in while this one is
+// transformed; with one slot (float, when two CTAs of two slots do not fit in
+// an SM's shared memory) the two CTAs on an SM overlap each other's copies.
 #pragma once
 #include <cuda.h>
 #include "gbfft_kernels.cuh"
@@ -47,8 +49,7 @@ __device__ __forceinline__ void rt_stages(Plan1D const &P, int t, bool active, c
     }
 }
 
-// float: compiled for two 512-thread CTAs per SM (64 registers, no spills):
-// with one tile slot the CTAs on an SM overlap each other's copies
+// float: compiled for two 512-thread CTAs per SM (64 registers, no spills)
 template<typename T, bool FWD, bool COLS, int LOADER>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
 k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtensorMap tmap){
