@@ -466,9 +466,10 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     int tpb = 1;
     size_t smem = 0;
     // tile slots: two (the copy of the next tile overlaps the transform of
-    // this one), or, for float when two CTAs of two slots do not fit in an
-    // SM's shared memory, one (the float kernel is compiled for two CTAs per
-    // SM, which then overlap each other's copies)
+    // this one), or, for float line tiles and for float column tiles whose
+    // two CTAs of two slots do not fit in an SM's shared memory, one (the
+    // float kernel is compiled for two CTAs per SM, which then overlap each
+    // other's copies; measured faster for line tiles at 384-640 points)
     int nbuf = 2;
     auto shape = [&](int nb){
         if (!cols){
@@ -484,7 +485,7 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
         }
     };
     shape(nbuf);
-    if (prec == 0 && !two_ctas_fit(smem)){
+    if (prec == 0 && (!cols || !two_ctas_fit(smem))){
         nbuf = 1;
         shape(nbuf);
     }

@@ -11,8 +11,9 @@
 //     is the stages' exchange layout, so every stage (stage 0 included) runs
 //     in place in the tile.
 // With two tile slots the next tile is copied in while this one is
-// transformed; with one slot (float, when two CTAs of two slots do not fit in
-// an SM's shared memory) the two CTAs on an SM overlap each other's copies.
+// transformed; with one slot (float line tiles, and float column tiles when
+// two CTAs of two slots do not fit in an SM's shared memory) the two CTAs on
+// an SM overlap each other's copies.
 #pragma once
 #include <cuda.h>
 #include "gbfft_kernels.cuh"
