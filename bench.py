@@ -484,6 +484,11 @@ WORKLOADS = {
     "z2z512fp64": ("c2c", (512, 512, 512), 1, False, "fp64"),
     "z2z512df": ("c2c", (512, 512, 512), 1, False, "double-float"),
     "c2c1024x1024x512": ("c2c", (1024, 1024, 512), 0),
+    # lengths that are not powers of two (runtime-radix pipelined passes)
+    "c2c384": ("c2c", (384, 384, 384), 0),
+    "c2c448": ("c2c", (448, 448, 448), 0),
+    "c2c480": ("c2c", (480, 480, 480), 0),
+    "c2c640x640x320": ("c2c", (640, 640, 320), 0),
     # the same two c2c float boxes with the radix-16 stages on the tensor cores
     "c2c512tc": ("c2c", (512, 512, 512), 0, True),
     "c2c1024x1024x512tc": ("c2c", (1024, 1024, 512), 0, True),
