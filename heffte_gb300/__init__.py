@@ -475,7 +475,9 @@ def r2r_prepost(prec, rkind, step, length, lines, in_ld, out_ld, src, dst, strea
 
 
 def set_kernel_variant(variant):
-    """0 automatic, 1 generic runtime-radix kernels, 2 pipelined kernels where they apply."""
+    """0 automatic, 1 generic runtime-radix kernels, 2 pipelined kernels where they
+    apply, 3 automatic with the runtime radix plan for every length that is not a
+    power of two (no kernels compiled for one length's plan)."""
     check(lib().heffte_gb300_set_kernel_variant(int(variant)))
 
 

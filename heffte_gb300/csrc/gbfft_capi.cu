@@ -65,7 +65,8 @@ int heffte_gb300_version(void){ return 10000; }
 
 int heffte_gb300_set_kernel_variant(int variant){
     return guard([&]{
-        if (variant < 0 || variant > 2) throw Error(ST_INVALID, "variant must be 0 (auto), 1 (generic) or 2 (pipelined)");
+        if (variant < 0 || variant > 3)
+            throw Error(ST_INVALID, "variant must be 0 (auto), 1 (generic), 2 (pipelined) or 3 (auto, runtime plans)");
         set_kernel_variant(variant);
     });
 }

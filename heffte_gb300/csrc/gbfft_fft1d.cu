@@ -291,6 +291,7 @@ static bool is_cols(Layout const &Li, Layout const &Lo){ return !(Li.estride == 
 
 static std::atomic<int> g_variant{0};
 int kernel_variant(){ return g_variant.load(); }
+bool rt_compiled_plans(){ return g_variant.load() != 3; }
 void set_kernel_variant(int v){ g_variant.store(v); }
 
 // double-float by default: 1.45x the FP64-instruction passes on GB300

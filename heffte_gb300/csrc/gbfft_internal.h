@@ -199,6 +199,11 @@ struct PipeRtParams {
 };
 void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
                     size_t smem, int threads);
+// float kernels compiled for the plan of length NC (gbfft_pipe_rt_n<NC>.cu);
+// false (nothing launched) when P.plan is not that plan
+template<int NC>
+bool launch_pipe_rt_ct(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap, size_t smem,
+                       int threads);
 
 // one dispatcher per precision and kind group (c2c / r2c+c2r / r2r), kind = K_*
 bool launch_pipe_f32_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
@@ -240,6 +245,8 @@ std::vector<int> pipe_radices(int N, bool df = false);
 // Kernel family selection (process-wide): 0 automatic, 1 generic runtime-radix
 // kernels only, 2 pipelined kernels wherever they apply.
 int kernel_variant();
+// whether float lengths with a compile-time plan kernel use it (variant != 3)
+bool rt_compiled_plans();
 void set_kernel_variant(int v);
 // Arithmetic of the pipelined complex<double> c2c passes (process-wide):
 // 0 FP64 instructions, 1 double-float pairs on the FP32 pipe.

@@ -1,56 +1,34 @@
 // Instantiations and launch of the pipelined runtime-radix complex kernels
 // (gbfft_pipe_rt.cuh): float and double, forward and backward, line tiles
-// (1-D bulk copies) and column tiles (3-D tensor-map copies).
-#include "gbfft_pipe_rt.cuh"
-#include <atomic>
+// (1-D bulk copies) and column tiles (3-D tensor-map copies).  Float
+// transforms of the lengths in kRtCtLengths run the kernels compiled for
+// that length's plan (gbfft_pipe_rt_n*.cu) when the plan is the default one.
+#include "gbfft_pipe_rt_launch.inl"
 
 namespace gbfft {
 
-namespace {
-
-template<typename T, bool FWD, bool COLS, int LOADER>
-void launch_one(cudaStream_t s, PipeRtParams const &P, CUtensorMap const &tmap, size_t smem, int threads){
-    auto kern = k_pipe_rt<T, FWD, COLS, LOADER>;
-    static std::atomic<unsigned long long> ready{0};
-    int dev = 0;
-    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-    unsigned long long bit = 1ull << (dev & 63);
-    if (!(ready.load() & bit)){
-        // the opt-in maximum per block less the kernel's static shared memory
-        int optin = 0;
-        check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device attribute");
-        cudaFuncAttributes fa{};
-        check_cuda(cudaFuncGetAttributes(&fa, kern), "function attributes");
-        check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
-                   "cudaFuncSetAttribute(pipelined runtime-radix kernel)");
-        ready.fetch_or(bit);
-    }
-    int nb = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem), "occupancy query");
-    long long grid = std::min<long long>(P.ntiles, (long long)num_sms() * std::max(nb, 1));
-    kern<<<(unsigned)grid, threads, smem, s>>>(P, tmap);
-    check_cuda(cudaPeekAtLastError(), "pipelined runtime-radix kernel launch");
-}
-
-template<typename T>
-void dispatch(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, CUtensorMap const &tmap, size_t smem,
-              int threads){
-    if (cols){
-        if (fwd) launch_one<T, true, true, RT_LD_TENSOR>(s, P, tmap, smem, threads);
-        else launch_one<T, false, true, RT_LD_TENSOR>(s, P, tmap, smem, threads);
-    } else {
-        if (fwd) launch_one<T, true, false, RT_LD_BULK>(s, P, tmap, smem, threads);
-        else launch_one<T, false, false, RT_LD_BULK>(s, P, tmap, smem, threads);
+static bool launch_ct(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap, size_t smem,
+                      int threads){
+    switch (P.plan.N){
+        case 320: return launch_pipe_rt_ct<320>(s, fwd, cols, P, tmap, smem, threads);
+        case 384: return launch_pipe_rt_ct<384>(s, fwd, cols, P, tmap, smem, threads);
+        case 448: return launch_pipe_rt_ct<448>(s, fwd, cols, P, tmap, smem, threads);
+        case 480: return launch_pipe_rt_ct<480>(s, fwd, cols, P, tmap, smem, threads);
+        case 640: return launch_pipe_rt_ct<640>(s, fwd, cols, P, tmap, smem, threads);
+        case 768: return launch_pipe_rt_ct<768>(s, fwd, cols, P, tmap, smem, threads);
+        default: return false;
     }
 }
-
-} // namespace
 
 void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
                     size_t smem, int threads){
     CUtensorMap const &m = *reinterpret_cast<CUtensorMap const*>(tmap);
-    if (prec == 0) dispatch<float>(s, fwd, cols, P, m, smem, threads);
-    else dispatch<double>(s, fwd, cols, P, m, smem, threads);
+    if (prec == 0){
+        if (rt_compiled_plans() && launch_ct(s, fwd, cols, P, tmap, smem, threads)) return;
+        dispatch<float, 0>(s, fwd, cols, P, m, smem, threads);
+    } else {
+        dispatch<double, 0>(s, fwd, cols, P, m, smem, threads);
+    }
 }
 
 } // namespace gbfft

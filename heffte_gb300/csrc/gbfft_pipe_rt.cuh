@@ -50,15 +50,144 @@ __device__ __forceinline__ void rt_stages(Plan1D const &P, int t, bool active, c
     }
 }
 
-// float: compiled for two 512-thread CTAs per SM (64 registers, no spills)
-template<typename T, bool FWD, bool COLS, int LOADER>
+// Compile-time radix plan of one length, built by the rule of the host's
+// plan builder for lengths that are not powers of two (radix-16 stages first,
+// the rest of the power of two as 8x4, 8, 4 or 2, then the odd primes 13,
+// 11, 7, 5, 3; twiddle offsets of the Stockham table; threads per transform
+// the most that any stage needs at `emax` values per thread).  The host runs
+// a compile-time kernel only when its runtime plan equals this one
+// (ct_plan_matches).
+struct CtPlan {
+    int N, T, nstages;
+    int R[kMaxStages], Ns[kMaxStages], NR[kMaxStages], tw[kMaxStages];
+};
+
+__host__ __device__ constexpr CtPlan ct_plan(int N, int emax){
+    CtPlan p{};
+    p.N = N; p.T = 1; p.nstages = 0;
+    if (N <= 1) return p;
+    int odd[kMaxStages] = {};
+    int nodd = 0, n = N;
+    int const primes[5] = {13, 11, 7, 5, 3};
+    for (int i = 0; i < 5; i++)
+        while (n % primes[i] == 0){ odd[nodd++] = primes[i]; n /= primes[i]; }
+    int a = 0;
+    while (n % 2 == 0){ n /= 2; a++; }
+    if (n != 1) return p;                     // a prime factor without a butterfly: no plan
+    int rad[kMaxStages] = {};
+    int ns = 0, q = a / 4, rem = a % 4;
+    int tail[2] = {0, 0}, ntail = 0;
+    if (rem == 1 && q >= 1){ q -= 1; tail[0] = 8; tail[1] = 4; ntail = 2; }
+    else if (rem == 1){ tail[0] = 2; ntail = 1; }
+    else if (rem == 2){ tail[0] = 4; ntail = 1; }
+    else if (rem == 3){ tail[0] = 8; ntail = 1; }
+    for (int i = 0; i < q; i++) rad[ns++] = 16;
+    for (int i = 0; i < ntail; i++) rad[ns++] = tail[i];
+    for (int i = 0; i < nodd; i++) rad[ns++] = odd[i];
+    int Ns = 1, off = 0, T = 1;
+    for (int s = 0; s < ns; s++){
+        int R = rad[s];
+        p.R[s] = R; p.Ns[s] = Ns; p.NR[s] = N / R; p.tw[s] = off;
+        if (s > 0) off += Ns * (R - 1);
+        int per = emax / R;
+        int need = (N / R + per - 1) / per;
+        if (need > T) T = need;
+        Ns *= R;
+    }
+    p.nstages = ns;
+    p.T = T;
+    return p;
+}
+
+// Whether the runtime plan of a transform is the compile-time plan of NC.
+template<int NC>
+inline bool ct_plan_matches(Plan1D const &P){
+    constexpr CtPlan c = ct_plan(NC, kEmax);
+    if (c.nstages == 0 || P.N != NC || P.nstages != c.nstages || P.T != c.T) return false;
+    for (int s = 0; s < c.nstages; s++)
+        if (P.st[s].R != c.R[s] || P.st[s].Ns != c.Ns[s] || P.st[s].NR != c.NR[s] || P.st[s].tw != c.tw[s])
+            return false;
+    return true;
+}
+
+// One Stockham stage with every size a constant: radix R, NS = product of
+// the previous radices, NR = N / R butterflies, TWO = the stage's twiddle
+// offset, TT threads per transform (each owns butterflies t, t + TT, ...).
+// FIRST: stage 0 of line tiles, read from the unpadded tile by `ld`; TG: the
+// last stage, stored to global memory by `st`.  Otherwise the exchange of
+// fft_stage (gbfft_kernels.cuh).
+template<int R, int NS, int NR, int TWO, int TT, int EMAX, bool FWD, bool COLS, bool FIRST, bool TG, typename T,
+         class LD, class ST>
+__device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
+                                             c_t<T> const *__restrict__ tw, Regs<T, EMAX> &r, LD &ld, ST &st){
+    using C = c_t<T>;
+    constexpr int MU = (NR + TT - 1) / TT;            // butterflies per thread, at most
+    static_assert(MU * R <= EMAX, "stage does not fit the register file");
+    #pragma unroll
+    for (int m = 0; m < MU; m++){
+        int j = t + m * TT;
+        if (active && ((m + 1) * TT <= NR || j < NR)){
+            #pragma unroll
+            for (int q = 0; q < R; q++){
+                if constexpr (FIRST) r.v[m * R + q] = ld(j + q * NR);
+                else r.v[m * R + q] = sm[sm_index<COLS>(j + q * NR, loc, TPB, padn)];
+            }
+        }
+    }
+    if constexpr (!FIRST) __syncthreads();
+    #pragma unroll
+    for (int m = 0; m < MU; m++){
+        int j = t + m * TT;
+        if (active && ((m + 1) * TT <= NR || j < NR)){
+            int hi = j / NS;
+            int k = j - hi * NS;
+            if constexpr (NS > 1){
+                if (k != 0){
+                    C const *w = tw + TWO + k * (R - 1);
+                    #pragma unroll
+                    for (int q = 1; q < R; q++){
+                        C wq = __ldg(w + q - 1);
+                        r.v[m * R + q] = FWD ? cmul(r.v[m * R + q], wq) : cmulc(r.v[m * R + q], wq);
+                    }
+                }
+            }
+            bfly<R, FWD, C, T>(&r.v[m * R]);
+            int ob = hi * NS * R + k;
+            #pragma unroll
+            for (int q = 0; q < R; q++){
+                if constexpr (TG) st(ob + q * NS, r.v[m * R + q]);
+                else sm[sm_index<COLS>(ob + q * NS, loc, TPB, padn)] = r.v[m * R + q];
+            }
+        }
+    }
+    if constexpr (!TG) __syncthreads();
+}
+
+// Stages S.. of the compile-time plan of NC.
+template<int NC, int S, int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+__device__ __forceinline__ void rt_stages_ct(int t, bool active, c_t<T> *sm_x, int loc, int TPB, int padn,
+                                             c_t<T> const *__restrict__ tw, Regs<T, EMAX> &r, LD &ld, ST &st){
+    constexpr CtPlan P = ct_plan(NC, EMAX);
+    if constexpr (S < P.nstages){
+        fft_stage_ct<P.R[S], P.Ns[S], P.NR[S], P.tw[S], P.T, EMAX, FWD, COLS, !COLS && S == 0, S == P.nstages - 1, T>(
+            t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
+        rt_stages_ct<NC, S + 1, EMAX, FWD, COLS, T>(t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
+    }
+}
+
+// float: compiled for two 512-thread CTAs per SM (64 registers, no spills).
+// NC: 0 for the runtime plan, else the length whose compile-time plan the
+// stages run (constant sizes, divisions and trip counts).
+template<typename T, bool FWD, bool COLS, int LOADER, int NC>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
 k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
     constexpr int EMAX = kEmax;
+    constexpr int TC = ct_plan(NC, EMAX).T;
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ __align__(8) uint64_t bar[2];
-    int const N = P.plan.N, TPB = P.tpb;
+    int const N = NC ? NC : P.plan.N, TPB = P.tpb;
+    int const Tt = NC ? TC : P.plan.T;
     int const padn = padded_len(N);
     long long const TILE = (long long)TPB * N;             // complex values per tile buffer
     C *tiles = reinterpret_cast<C*>(smraw);
@@ -66,7 +195,7 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
     C *xline = tiles + nbuf * TILE;                        // line tiles: padded exchange buffer
     int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     int loc, t;
-    thread_map<COLS>(TPB, P.plan.T, loc, t);
+    thread_map<COLS>(TPB, Tt, loc, t);
     Layout const Li = P.Li, Lo = P.Lo;
 
     if (tid == 0){
@@ -139,12 +268,17 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
             valid = g < P.G;
             if (valid) oa = base_of(Lo, g);
         }
-        active = valid && (t < P.plan.T) && (loc < TPB);
+        active = valid && (t < Tt) && (loc < TPB);
         C *out = reinterpret_cast<C*>(P.out);
         long long const oes = Lo.estride;
         auto ld = [&](int p) -> C { return tb[(long long)loc * N + p]; };
         auto st = [&](int p, C x){ out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
-        rt_stages<EMAX, FWD, COLS, T>(P.plan, t, active, COLS ? tb : xline, loc, TPB, padn, tw, ld, st);
+        if constexpr (NC != 0){
+            Regs<T, EMAX> r;
+            rt_stages_ct<NC, 0, EMAX, FWD, COLS, T>(t, active, COLS ? tb : xline, loc, TPB, padn, tw, r, ld, st);
+        } else {
+            rt_stages<EMAX, FWD, COLS, T>(P.plan, t, active, COLS ? tb : xline, loc, TPB, padn, tw, ld, st);
+        }
         __syncthreads();
     }
 }

@@ -455,6 +455,29 @@ def test_power_of_two_kernel_variants(gb, variant, prec):
         gb.set_kernel_variant(0)
 
 
+@pytest.mark.parametrize("variant", [0, 3])
+def test_compiled_plan_lengths(gb, variant):
+    """The float lengths with kernels compiled for their radix plan (320, 384,
+    448, 480, 640, 768; variant 0) and the same lengths on the runtime radix
+    plan (variant 3): the length along each dimension (line tiles, column
+    tiles), partial tiles, three orders, forward and backward."""
+    gb.set_kernel_variant(variant)
+    try:
+        rng = np.random.default_rng(70 + variant)
+        for N in (320, 384, 448, 480, 640, 768):
+            for size in [(N, 13, 3), (5, N, 7), (3, 11, N)]:
+                n = int(np.prod(size))
+                x = rand_c(rng, n, 0)
+                for io, oo in [((0, 1, 2), (0, 1, 2)), ((2, 1, 0), (2, 1, 0)), ((1, 0, 2), (0, 2, 1))]:
+                    y = run_c2c(gb, x, size, io, oo, 0, 1, 0)
+                    assert O.rel_l2(y, O.fft3d_c2c(x, size, io, oo, 0, 1)) < TOL[0], (N, size, io, oo)
+                    z = run_c2c(gb, y, size, io, oo, 1, 0, 0)
+                    assert O.rel_l2(z, x) < 3 * TOL[0], (N, size, io, oo, "backward")
+        assert gb.device_status() == 0
+    finally:
+        gb.set_kernel_variant(0)
+
+
 @pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("prec", [0, 1])
 def test_power_of_two_real_kernel_variants(gb, variant, prec):
