@@ -38,6 +38,9 @@ def parse():
     ap.add_argument("--prec", default="single", choices=["single", "double"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="", help="report other configurations: a name, a comma list or 'all'")
+    ap.add_argument("--kernel-variant", type=int, default=0,
+                    help="--workload lines: kernel family (heffte_gb300_set_kernel_variant; 3 = lengths that "
+                         "are not powers of two on the runtime radix plan)")
     return ap.parse_args()
 
 
@@ -929,8 +932,14 @@ def run_workload_plain(name, steps, warmup, kind, size, prec, tc):
 def main():
     args = parse()
     if args.workload:
+        if args.kernel_variant:
+            import heffte_gb300 as gb
+            gb.set_kernel_variant(args.kernel_variant)
         for name in (WORKLOADS if args.workload == "all" else args.workload.split(",")):
-            print(json.dumps(run_workload(name, args.steps, args.warmup)), flush=True)
+            out = run_workload(name, args.steps, args.warmup)
+            if args.kernel_variant:
+                out["kernel_variant"] = args.kernel_variant
+            print(json.dumps(out), flush=True)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
