@@ -471,18 +471,21 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     // two CTAs of two slots do not fit in an SM's shared memory, one (the
     // float kernel is compiled for two CTAs per SM, which then overlap each
     // other's copies; measured faster for line tiles at 384-640 points)
+    // the twiddle table of a kernel compiled for this plan (float), in
+    // shared memory after the tiles
+    size_t const extra = (prec == 0) ? rt_ct_smem(f.plan) : 0;
     int nbuf = 2;
     auto shape = [&](int nb){
         if (!cols){
             tpb = std::max(1, 256 / T);
             while (tpb > 1 && tpb * T > 512) tpb /= 2;
-            while (tpb > 1 && (nb * (size_t)tpb * N + (size_t)tpb * padn) * es > 200 * 1024) tpb /= 2;
-            smem = (nb * (size_t)tpb * N + (size_t)tpb * padn) * es;
+            while (tpb > 1 && (nb * (size_t)tpb * N + (size_t)tpb * padn) * es + extra > 200 * 1024) tpb /= 2;
+            smem = (nb * (size_t)tpb * N + (size_t)tpb * padn) * es + extra;
         } else {
             tpb = (prec == 0) ? 16 : 8;
             while (tpb > 2 && tpb * T > 512) tpb /= 2;
-            while (tpb > 2 && nb * (size_t)tpb * N * es > 200 * 1024) tpb /= 2;
-            smem = nb * (size_t)tpb * N * es;
+            while (tpb > 2 && nb * (size_t)tpb * N * es + extra > 200 * 1024) tpb /= 2;
+            smem = nb * (size_t)tpb * N * es + extra;
         }
     };
     shape(nbuf);
@@ -523,6 +526,7 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     P.G = G;
     P.tpb = tpb;
     P.nbuf = nbuf;
+    P.ct = (extra > 0) ? 1 : 0;
     P.scale = scale;
     P.do_scale = (scale != 1.0);
     P.status = device_status();

@@ -191,6 +191,7 @@ struct PipeRtParams {
     long long tiles_per_block;   // column tiles covering one block of `count` columns
     int tpb;                     // transforms per tile
     int nbuf;                    // tile slots: 2 (the next tile copied while one is transformed) or 1
+    int ct;                      // float: run the kernel compiled for the plan (smem includes its twiddles)
     int boxr;                    // rows per tensor-map copy (divides N)
     int tswap;
     double scale;
@@ -199,6 +200,9 @@ struct PipeRtParams {
 };
 void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
                     size_t smem, int threads);
+// shared-memory bytes that the float kernel compiled for this plan adds to
+// the tiles (its twiddle table), 0 when no compiled kernel runs it
+size_t rt_ct_smem(Plan1D const &plan);
 // float kernels compiled for the plan of length NC (gbfft_pipe_rt_n<NC>.cu);
 // false (nothing launched) when P.plan is not that plan
 template<int NC>

@@ -7,6 +7,24 @@
 
 namespace gbfft {
 
+template<int NC>
+static size_t ct_smem(Plan1D const &plan){
+    return ct_plan_matches<NC>(plan) ? (size_t)ct_twiddles(NC, kEmax) * sizeof(float2) : 0;
+}
+
+size_t rt_ct_smem(Plan1D const &plan){
+    if (!rt_compiled_plans()) return 0;
+    switch (plan.N){
+        case 320: return ct_smem<320>(plan);
+        case 384: return ct_smem<384>(plan);
+        case 448: return ct_smem<448>(plan);
+        case 480: return ct_smem<480>(plan);
+        case 640: return ct_smem<640>(plan);
+        case 768: return ct_smem<768>(plan);
+        default: return 0;
+    }
+}
+
 static bool launch_ct(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap, size_t smem,
                       int threads){
     switch (P.plan.N){
@@ -24,7 +42,8 @@ void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams 
                     size_t smem, int threads){
     CUtensorMap const &m = *reinterpret_cast<CUtensorMap const*>(tmap);
     if (prec == 0){
-        if (rt_compiled_plans() && launch_ct(s, fwd, cols, P, tmap, smem, threads)) return;
+        // P.ct: the shared memory was sized for the compiled kernel's twiddles
+        if (P.ct && launch_ct(s, fwd, cols, P, tmap, smem, threads)) return;
         dispatch<float, 0>(s, fwd, cols, P, m, smem, threads);
     } else {
         dispatch<double, 0>(s, fwd, cols, P, m, smem, threads);

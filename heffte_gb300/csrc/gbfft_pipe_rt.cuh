@@ -99,6 +99,15 @@ __host__ __device__ constexpr CtPlan ct_plan(int N, int emax){
     return p;
 }
 
+// Twiddles of the compile-time plan of N (complex values): stage s > 0 holds
+// Ns * (R - 1) of them.
+__host__ __device__ constexpr int ct_twiddles(int N, int emax){
+    CtPlan const p = ct_plan(N, emax);
+    int n = 0;
+    for (int s = 1; s < p.nstages; s++) n += p.Ns[s] * (p.R[s] - 1);
+    return n;
+}
+
 // Whether the runtime plan of a transform is the compile-time plan of NC.
 template<int NC>
 inline bool ct_plan_matches(Plan1D const &P){
@@ -115,11 +124,14 @@ inline bool ct_plan_matches(Plan1D const &P){
 // offset, TT threads per transform (each owns butterflies t, t + TT, ...).
 // FIRST: stage 0 of line tiles, read from the unpadded tile by `ld`; TG: the
 // last stage, stored to global memory by `st`.  Otherwise the exchange of
-// fft_stage (gbfft_kernels.cuh).
+// fft_stage (gbfft_kernels.cuh).  tws: the twiddle table in shared memory,
+// each stage's block transposed to [q - 1][k] (twiddle q of butterfly
+// column k at TWO + (q - 1) * NS + k), so that a warp's threads, which hold
+// consecutive k, read consecutive entries.
 template<int R, int NS, int NR, int TWO, int TT, int EMAX, bool FWD, bool COLS, bool FIRST, bool TG, typename T,
          class LD, class ST>
 __device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
-                                             c_t<T> const *__restrict__ tw, Regs<T, EMAX> &r, LD &ld, ST &st){
+                                             c_t<T> const *tws, Regs<T, EMAX> &r, LD &ld, ST &st){
     using C = c_t<T>;
     constexpr int MU = (NR + TT - 1) / TT;            // butterflies per thread, at most
     static_assert(MU * R <= EMAX, "stage does not fit the register file");
@@ -143,10 +155,10 @@ __device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int
             int k = j - hi * NS;
             if constexpr (NS > 1){
                 if (k != 0){
-                    C const *w = tw + TWO + k * (R - 1);
+                    C const *w = tws + TWO + k;
                     #pragma unroll
                     for (int q = 1; q < R; q++){
-                        C wq = __ldg(w + q - 1);
+                        C wq = w[(q - 1) * NS];
                         r.v[m * R + q] = FWD ? cmul(r.v[m * R + q], wq) : cmulc(r.v[m * R + q], wq);
                     }
                 }
@@ -166,12 +178,27 @@ __device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int
 // Stages S.. of the compile-time plan of NC.
 template<int NC, int S, int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
 __device__ __forceinline__ void rt_stages_ct(int t, bool active, c_t<T> *sm_x, int loc, int TPB, int padn,
-                                             c_t<T> const *__restrict__ tw, Regs<T, EMAX> &r, LD &ld, ST &st){
+                                             c_t<T> const *tw, Regs<T, EMAX> &r, LD &ld, ST &st){
     constexpr CtPlan P = ct_plan(NC, EMAX);
     if constexpr (S < P.nstages){
         fft_stage_ct<P.R[S], P.Ns[S], P.NR[S], P.tw[S], P.T, EMAX, FWD, COLS, !COLS && S == 0, S == P.nstages - 1, T>(
             t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
         rt_stages_ct<NC, S + 1, EMAX, FWD, COLS, T>(t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
+    }
+}
+
+// Copies the twiddles of stages S.. of the compile-time plan of NC from the
+// Stockham table (stage block [k][q - 1]) to shared memory ([q - 1][k]).
+template<int NC, int S, int EMAX, typename C>
+__device__ __forceinline__ void ct_copy_twiddles(C *tws, C const *__restrict__ tw){
+    constexpr CtPlan P = ct_plan(NC, EMAX);
+    if constexpr (S < P.nstages){
+        constexpr int R1 = P.R[S] - 1, NS = P.Ns[S], TWO = P.tw[S];
+        for (int i = threadIdx.x; i < NS * R1; i += blockDim.x){
+            int k = i / R1, q1 = i - k * R1;
+            tws[TWO + q1 * NS + k] = __ldg(tw + TWO + i);
+        }
+        ct_copy_twiddles<NC, S + 1, EMAX>(tws, tw);
     }
 }
 
@@ -204,6 +231,10 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
         fence_mbar_init();
         if (LOADER == RT_LD_TENSOR) prefetch_tmap(&tmap);
     }
+    // compile-time plans: the twiddle table, transposed per stage, after the
+    // tile slots (and the exchange buffer of line tiles)
+    C *tws = tiles + nbuf * TILE + (COLS ? 0 : (long long)TPB * padn);
+    if constexpr (NC != 0) ct_copy_twiddles<NC, 1, EMAX>(tws, reinterpret_cast<C const*>(P.tw));
     __syncthreads();
 
     auto tile_origin = [&](long long tile, long long &blk, long long &c0){
@@ -275,7 +306,7 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
         auto st = [&](int p, C x){ out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
         if constexpr (NC != 0){
             Regs<T, EMAX> r;
-            rt_stages_ct<NC, 0, EMAX, FWD, COLS, T>(t, active, COLS ? tb : xline, loc, TPB, padn, tw, r, ld, st);
+            rt_stages_ct<NC, 0, EMAX, FWD, COLS, T>(t, active, COLS ? tb : xline, loc, TPB, padn, tws, r, ld, st);
         } else {
             rt_stages<EMAX, FWD, COLS, T>(P.plan, t, active, COLS ? tb : xline, loc, TPB, padn, tw, ld, st);
         }
