@@ -467,14 +467,15 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     int tpb = 1;
     size_t smem = 0;
     // tile slots: two (the copy of the next tile overlaps the transform of
-    // this one), or, for float line tiles and for float column tiles whose
-    // two CTAs of two slots do not fit in an SM's shared memory, one (the
-    // float kernel is compiled for two CTAs per SM, which then overlap each
-    // other's copies; measured faster for line tiles at 384-640 points)
-    // the twiddle table of a kernel compiled for this plan (float), in
-    // shared memory after the tiles
+    // this one), or one for float line tiles (the float kernel is compiled
+    // for two CTAs per SM, which then overlap each other's copies; measured
+    // faster for line tiles at 384-640 points).  Float column tiles keep two
+    // slots where two CTAs of them fit in an SM's shared memory, with 16
+    // columns, else with 8 (even N), else take one slot of 16 columns.  `extra`: the
+    // twiddle table of a kernel compiled for this plan (float), in shared
+    // memory after the tiles.
     size_t const extra = (prec == 0) ? rt_ct_smem(f.plan) : 0;
-    int nbuf = 2;
+    int nbuf = 2, cap = 16;
     auto shape = [&](int nb){
         if (!cols){
             tpb = std::max(1, 256 / T);
@@ -482,16 +483,27 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
             while (tpb > 1 && (nb * (size_t)tpb * N + (size_t)tpb * padn) * es + extra > 200 * 1024) tpb /= 2;
             smem = (nb * (size_t)tpb * N + (size_t)tpb * padn) * es + extra;
         } else {
-            tpb = (prec == 0) ? 16 : 8;
+            tpb = (prec == 0) ? cap : 8;
             while (tpb > 2 && tpb * T > 512) tpb /= 2;
             while (tpb > 2 && nb * (size_t)tpb * N * es + extra > 200 * 1024) tpb /= 2;
             smem = nb * (size_t)tpb * N * es + extra;
         }
     };
     shape(nbuf);
-    if (prec == 0 && (!cols || !two_ctas_fit(smem))){
+    if (prec == 0 && !cols){
         nbuf = 1;
         shape(nbuf);
+    } else if (prec == 0 && !two_ctas_fit(smem)){
+        // 8 columns are 64 bytes per row, so a copy's rows (a divisor of N)
+        // must be even for its 128-byte aligned destination: even N only
+        if (N % 2 == 0){
+            cap = 8;
+            shape(nbuf);
+        }
+        if (!two_ctas_fit(smem)){
+            nbuf = 1; cap = 16;
+            shape(nbuf);
+        }
     }
     if (!cols){
         if (Li.dist != N || (G > Li.count && Li.bstride != Li.count * N)) return false;
