@@ -470,11 +470,14 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     // this one), or one for float line tiles (the float kernel is compiled
     // for two CTAs per SM, which then overlap each other's copies; measured
     // faster for line tiles at 384-640 points).  Float column tiles keep two
-    // slots where two CTAs of them fit in an SM's shared memory, with 16
-    // columns, else with 8 (even N), else take one slot of 16 columns.  `extra`: the
-    // twiddle table of a kernel compiled for this plan (float), in shared
-    // memory after the tiles.
-    size_t const extra = (prec == 0) ? rt_ct_smem(f.plan) : 0;
+    // slots where two CTAs of them fit in an SM's shared memory: 16 columns;
+    // else 16 columns with a compiled kernel's twiddles left in global
+    // memory; else 8 columns (even N); else one slot of 16 columns.  `extra`:
+    // the twiddle table of a kernel compiled for this plan (float), in shared
+    // memory after the tiles (ct 1), or 0 (ct 2: in global memory).
+    size_t const ctb = (prec == 0) ? rt_ct_smem(f.plan) : 0;
+    size_t extra = ctb;
+    int ct = (ctb > 0) ? 1 : 0;
     int nbuf = 2, cap = 16;
     auto shape = [&](int nb){
         if (!cols){
@@ -494,13 +497,21 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
         nbuf = 1;
         shape(nbuf);
     } else if (prec == 0 && !two_ctas_fit(smem)){
+        bool fit = false;
+        if (ctb > 0){
+            extra = 0;
+            shape(nbuf);
+            fit = two_ctas_fit(smem);
+            if (fit) ct = 2; else extra = ctb;
+        }
         // 8 columns are 64 bytes per row, so a copy's rows (a divisor of N)
         // must be even for its 128-byte aligned destination: even N only
-        if (N % 2 == 0){
+        if (!fit && N % 2 == 0){
             cap = 8;
             shape(nbuf);
+            fit = two_ctas_fit(smem);
         }
-        if (!two_ctas_fit(smem)){
+        if (!fit){
             nbuf = 1; cap = 16;
             shape(nbuf);
         }
@@ -538,7 +549,7 @@ static bool try_pipe_rt(cudaStream_t s, Fft1D &f, int prec, bool fwd, Layout Li,
     P.G = G;
     P.tpb = tpb;
     P.nbuf = nbuf;
-    P.ct = (extra > 0) ? 1 : 0;
+    P.ct = ct;
     P.scale = scale;
     P.do_scale = (scale != 1.0);
     P.status = device_status();

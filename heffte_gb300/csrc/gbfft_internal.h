@@ -191,7 +191,8 @@ struct PipeRtParams {
     long long tiles_per_block;   // column tiles covering one block of `count` columns
     int tpb;                     // transforms per tile
     int nbuf;                    // tile slots: 2 (the next tile copied while one is transformed) or 1
-    int ct;                      // float: run the kernel compiled for the plan (smem includes its twiddles)
+    int ct;                      // float: the kernel compiled for the plan, 1 twiddles in shared memory
+                                 // (smem includes them), 2 in global memory; 0 the runtime-plan kernel
     int boxr;                    // rows per tensor-map copy (divides N)
     int tswap;
     double scale;

@@ -42,11 +42,12 @@ void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams 
                     size_t smem, int threads){
     CUtensorMap const &m = *reinterpret_cast<CUtensorMap const*>(tmap);
     if (prec == 0){
-        // P.ct: the shared memory was sized for the compiled kernel's twiddles
+        // P.ct: a compiled kernel, with its twiddles in shared memory (1, counted
+        // in smem) or in global memory (2)
         if (P.ct && launch_ct(s, fwd, cols, P, tmap, smem, threads)) return;
-        dispatch<float, 0>(s, fwd, cols, P, m, smem, threads);
+        dispatch<float, 0, false>(s, fwd, cols, P, m, smem, threads);
     } else {
-        dispatch<double, 0>(s, fwd, cols, P, m, smem, threads);
+        dispatch<double, 0, false>(s, fwd, cols, P, m, smem, threads);
     }
 }
 

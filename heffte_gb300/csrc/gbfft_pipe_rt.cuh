@@ -124,14 +124,15 @@ inline bool ct_plan_matches(Plan1D const &P){
 // offset, TT threads per transform (each owns butterflies t, t + TT, ...).
 // FIRST: stage 0 of line tiles, read from the unpadded tile by `ld`; TG: the
 // last stage, stored to global memory by `st`.  Otherwise the exchange of
-// fft_stage (gbfft_kernels.cuh).  tws: the twiddle table in shared memory,
-// each stage's block transposed to [q - 1][k] (twiddle q of butterfly
-// column k at TWO + (q - 1) * NS + k), so that a warp's threads, which hold
-// consecutive k, read consecutive entries.
-template<int R, int NS, int NR, int TWO, int TT, int EMAX, bool FWD, bool COLS, bool FIRST, bool TG, typename T,
-         class LD, class ST>
+// fft_stage (gbfft_kernels.cuh).  TWS: tw is the twiddle table in shared
+// memory, each stage's block transposed to [q - 1][k] (twiddle q of
+// butterfly column k at TWO + (q - 1) * NS + k), so that a warp's threads,
+// which hold consecutive k, read consecutive entries; else the Stockham
+// table in global memory ([k][q - 1]).
+template<int R, int NS, int NR, int TWO, int TT, int EMAX, bool FWD, bool COLS, bool FIRST, bool TG, bool TWS,
+         typename T, class LD, class ST>
 __device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
-                                             c_t<T> const *tws, Regs<T, EMAX> &r, LD &ld, ST &st){
+                                             c_t<T> const *tw, Regs<T, EMAX> &r, LD &ld, ST &st){
     using C = c_t<T>;
     constexpr int MU = (NR + TT - 1) / TT;            // butterflies per thread, at most
     static_assert(MU * R <= EMAX, "stage does not fit the register file");
@@ -155,10 +156,9 @@ __device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int
             int k = j - hi * NS;
             if constexpr (NS > 1){
                 if (k != 0){
-                    C const *w = tws + TWO + k;
                     #pragma unroll
                     for (int q = 1; q < R; q++){
-                        C wq = w[(q - 1) * NS];
+                        C wq = TWS ? tw[TWO + (q - 1) * NS + k] : __ldg(tw + TWO + k * (R - 1) + q - 1);
                         r.v[m * R + q] = FWD ? cmul(r.v[m * R + q], wq) : cmulc(r.v[m * R + q], wq);
                     }
                 }
@@ -176,14 +176,14 @@ __device__ __forceinline__ void fft_stage_ct(int t, bool active, c_t<T> *sm, int
 }
 
 // Stages S.. of the compile-time plan of NC.
-template<int NC, int S, int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+template<int NC, int S, int EMAX, bool FWD, bool COLS, bool TWS, typename T, class LD, class ST>
 __device__ __forceinline__ void rt_stages_ct(int t, bool active, c_t<T> *sm_x, int loc, int TPB, int padn,
                                              c_t<T> const *tw, Regs<T, EMAX> &r, LD &ld, ST &st){
     constexpr CtPlan P = ct_plan(NC, EMAX);
     if constexpr (S < P.nstages){
-        fft_stage_ct<P.R[S], P.Ns[S], P.NR[S], P.tw[S], P.T, EMAX, FWD, COLS, !COLS && S == 0, S == P.nstages - 1, T>(
-            t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
-        rt_stages_ct<NC, S + 1, EMAX, FWD, COLS, T>(t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
+        fft_stage_ct<P.R[S], P.Ns[S], P.NR[S], P.tw[S], P.T, EMAX, FWD, COLS, !COLS && S == 0, S == P.nstages - 1, TWS,
+                     T>(t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
+        rt_stages_ct<NC, S + 1, EMAX, FWD, COLS, TWS, T>(t, active, sm_x, loc, TPB, padn, tw, r, ld, st);
     }
 }
 
@@ -204,8 +204,10 @@ __device__ __forceinline__ void ct_copy_twiddles(C *tws, C const *__restrict__ t
 
 // float: compiled for two 512-thread CTAs per SM (64 registers, no spills).
 // NC: 0 for the runtime plan, else the length whose compile-time plan the
-// stages run (constant sizes, divisions and trip counts).
-template<typename T, bool FWD, bool COLS, int LOADER, int NC>
+// stages run (constant sizes, divisions and trip counts); TWS (NC != 0): its
+// twiddles copied to shared memory (the host adds their bytes), else read
+// from the global table.
+template<typename T, bool FWD, bool COLS, int LOADER, int NC, bool TWS>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
 k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
@@ -234,7 +236,7 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
     // compile-time plans: the twiddle table, transposed per stage, after the
     // tile slots (and the exchange buffer of line tiles)
     C *tws = tiles + nbuf * TILE + (COLS ? 0 : (long long)TPB * padn);
-    if constexpr (NC != 0) ct_copy_twiddles<NC, 1, EMAX>(tws, reinterpret_cast<C const*>(P.tw));
+    if constexpr (NC != 0 && TWS) ct_copy_twiddles<NC, 1, EMAX>(tws, reinterpret_cast<C const*>(P.tw));
     __syncthreads();
 
     auto tile_origin = [&](long long tile, long long &blk, long long &c0){
@@ -306,7 +308,8 @@ k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtens
         auto st = [&](int p, C x){ out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
         if constexpr (NC != 0){
             Regs<T, EMAX> r;
-            rt_stages_ct<NC, 0, EMAX, FWD, COLS, T>(t, active, COLS ? tb : xline, loc, TPB, padn, tws, r, ld, st);
+            rt_stages_ct<NC, 0, EMAX, FWD, COLS, TWS, T>(t, active, COLS ? tb : xline, loc, TPB, padn,
+                                                         TWS ? tws : tw, r, ld, st);
         } else {
             rt_stages<EMAX, FWD, COLS, T>(P.plan, t, active, COLS ? tb : xline, loc, TPB, padn, tw, ld, st);
         }

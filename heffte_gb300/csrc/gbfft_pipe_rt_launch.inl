@@ -9,9 +9,9 @@ namespace gbfft {
 
 namespace {
 
-template<typename T, bool FWD, bool COLS, int LOADER, int NC>
+template<typename T, bool FWD, bool COLS, int LOADER, int NC, bool TWS>
 void launch_one(cudaStream_t s, PipeRtParams const &P, CUtensorMap const &tmap, size_t smem, int threads){
-    auto kern = k_pipe_rt<T, FWD, COLS, LOADER, NC>;
+    auto kern = k_pipe_rt<T, FWD, COLS, LOADER, NC, TWS>;
     static std::atomic<unsigned long long> ready{0};
     int dev = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
@@ -33,15 +33,15 @@ void launch_one(cudaStream_t s, PipeRtParams const &P, CUtensorMap const &tmap, 
     check_cuda(cudaPeekAtLastError(), "pipelined runtime-radix kernel launch");
 }
 
-template<typename T, int NC>
+template<typename T, int NC, bool TWS>
 void dispatch(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, CUtensorMap const &tmap, size_t smem,
               int threads){
     if (cols){
-        if (fwd) launch_one<T, true, true, RT_LD_TENSOR, NC>(s, P, tmap, smem, threads);
-        else launch_one<T, false, true, RT_LD_TENSOR, NC>(s, P, tmap, smem, threads);
+        if (fwd) launch_one<T, true, true, RT_LD_TENSOR, NC, TWS>(s, P, tmap, smem, threads);
+        else launch_one<T, false, true, RT_LD_TENSOR, NC, TWS>(s, P, tmap, smem, threads);
     } else {
-        if (fwd) launch_one<T, true, false, RT_LD_BULK, NC>(s, P, tmap, smem, threads);
-        else launch_one<T, false, false, RT_LD_BULK, NC>(s, P, tmap, smem, threads);
+        if (fwd) launch_one<T, true, false, RT_LD_BULK, NC, TWS>(s, P, tmap, smem, threads);
+        else launch_one<T, false, false, RT_LD_BULK, NC, TWS>(s, P, tmap, smem, threads);
     }
 }
 
@@ -52,7 +52,10 @@ template<>
 bool launch_pipe_rt_ct<GBFFT_RT_LEN>(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
                                      size_t smem, int threads){
     if (!ct_plan_matches<GBFFT_RT_LEN>(P.plan)) return false;
-    dispatch<float, GBFFT_RT_LEN>(s, fwd, cols, P, *reinterpret_cast<CUtensorMap const*>(tmap), smem, threads);
+    CUtensorMap const &m = *reinterpret_cast<CUtensorMap const*>(tmap);
+    // P.ct: 1 twiddles in shared memory (counted in smem), 2 in global memory
+    if (P.ct == 1) dispatch<float, GBFFT_RT_LEN, true>(s, fwd, cols, P, m, smem, threads);
+    else dispatch<float, GBFFT_RT_LEN, false>(s, fwd, cols, P, m, smem, threads);
     return true;
 }
 #endif
