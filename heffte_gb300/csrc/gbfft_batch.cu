@@ -52,8 +52,9 @@ Batch::~Batch(){
     for (void *p : device_allocs) cudaFree(p);
 }
 
-static void const *batch_kernel(int prec, bool fwd, int values, bool r2c, bool s5){
+static void const *batch_kernel(int prec, bool fwd, int values, bool r2c, bool s5, bool twt){
     if (values == 8) return batch_kernel_e8(prec, fwd, r2c, s5);
+    if (twt) return batch_kernel_e16_r2c5_tw(fwd);
     if (r2c) return s5 ? batch_kernel_e16_r2c5(prec, fwd) : batch_kernel_e16_r2c(prec, fwd);
     return batch_kernel_e16_any(prec, fwd);
 }
@@ -352,9 +353,19 @@ std::unique_ptr<Batch> make_batch(int kind, int prec, std::vector<std::array<int
     smem = (smem + 15) / 16 * 16;
     b->pf_offset = (config.prefetch && pf_bytes > 0) ? (int)smem : -1;
     if (b->pf_offset > 0) smem += (pf_bytes + 15) / 16 * 16;
+    // the twiddle tables of all plans in shared memory (the float r2c kernel
+    // of 5-smooth plans with 16 values per thread), when they are few and small
+    size_t tw_total = 0;
+    for (Plan1D const &P : plans)
+        for (int s = 1; s < P.nstages; s++) tw_total += (size_t)P.st[s].Ns * (P.st[s].R - 1);
+    bool const twt = prec == 0 && values == 16 && kind == PK_R2C && s5 && (int)plans.size() <= kBatchTwPlans &&
+                     tw_total * csize <= 24 * 1024;
+    b->nplans = (int)plans.size();
+    b->tw_off = twt ? (int)smem : -1;
+    if (twt) smem += (tw_total * csize + 15) / 16 * 16;
     b->smem = smem;
     for (bool fwd : {true, false}){
-        void const *kern = batch_kernel(prec, fwd, values, kind == PK_R2C, s5);
+        void const *kern = batch_kernel(prec, fwd, values, kind == PK_R2C, s5, b->tw_off > 0);
         int nb_sm = 1;
         check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
         check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_sm, kern, kBatchThreads, smem), "occupancy");
@@ -388,9 +399,10 @@ static void build_graph(Batch &b, bool fwd){
     b.args_scaling = 0;
     b.args_budget = dependency_wait_budget();
     void *args[] = {&b.args_units, &b.args_nunits, &b.args_plans, &b.args_tws, &b.args_bufs, &b.args_counter,
-                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget, &b.pf_offset};
+                    &b.args_done, &b.args_total, &b.args_status, &b.args_scaling, &b.args_budget, &b.pf_offset,
+                    &b.nplans, &b.tw_off};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values, b.kind == PK_R2C, b.s5));
+    kp.func = const_cast<void*>(batch_kernel(b.prec, fwd, b.values, b.kind == PK_R2C, b.s5, b.tw_off > 0));
     kp.gridDim = dim3((unsigned)(fwd ? b.grid : b.grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)b.smem;
@@ -485,9 +497,9 @@ void Batch::run(bool fwd, void const *in, void *out, void *work, int scaling){
     args_scaling = scaling;
     args_budget = dependency_wait_budget();
     void *args[] = {&args_units, &args_nunits, &args_plans, &args_tws, &args_bufs, &args_counter, &args_done,
-                    &args_total, &args_status, &args_scaling, &args_budget, &pf_offset};
+                    &args_total, &args_status, &args_scaling, &args_budget, &pf_offset, &nplans, &tw_off};
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values, kind == PK_R2C, s5));
+    kp.func = const_cast<void*>(batch_kernel(prec, fwd, values, kind == PK_R2C, s5, tw_off > 0));
     kp.gridDim = dim3((unsigned)(fwd ? grid : grid_bwd));
     kp.blockDim = dim3(kBatchThreads);
     kp.sharedMemBytes = (unsigned)smem;

@@ -68,6 +68,8 @@ struct Batch {
     int pf_offset = -1;    // byte offset of the prefetch buffer in dynamic shared memory (-1: none)
     int values = 16;       // complex values per thread of the kernel in use (8 or 16)
     bool s5 = false;       // every radix plan 5-smooth (the kernels without radix 7, 11, 13)
+    int tw_off = -1;       // byte offset of the twiddle tables in dynamic shared memory (-1: read from global memory)
+    int nplans = 0;        // radix plans of the batch (entries of the plan and twiddle tables)
     int grid = 0;          // persistent CTAs of the forward kernel
     int grid_bwd = 0;      // and of the backward kernel
     cudaGraph_t fwd_graph = nullptr, bwd_graph = nullptr;

@@ -11,4 +11,9 @@ void const *batch_kernel_e16_r2c5(int prec, bool fwd){
                : reinterpret_cast<void const*>(k_batch<double, false, 16, true, true>);
 }
 
+void const *batch_kernel_e16_r2c5_tw(bool fwd){
+    return fwd ? reinterpret_cast<void const*>(k_batch<float, true, 16, true, true, true>)
+               : reinterpret_cast<void const*>(k_batch<float, false, 16, true, true, true>);
+}
+
 } // namespace gbfft

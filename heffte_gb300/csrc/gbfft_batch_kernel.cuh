@@ -114,14 +114,46 @@ template<class F> struct PrefetchHook {
 // kernel of c2c batches (c2c line and column tiles)
 // S5: every radix plan of the batch is 5-smooth (radices 2, 3, 4, 5, 8, 16):
 // the stages of radix 7, 11 and 13 are not compiled (fewer registers)
-template<typename T, bool FWD, int EMAX, bool R2C, bool S5>
+// TWT: every CTA first copies the twiddle tables of all nplans plans into
+// shared memory at byte offset tw_off (at most kBatchTwPlans plans), each
+// stage's block transposed to [q - 1][k] so that a warp reads consecutive
+// entries; the stages read them there instead of from global memory
+constexpr int kBatchTwPlans = 64;
+template<typename T, bool FWD, int EMAX, bool R2C, bool S5, bool TWT = false>
 __global__ void __launch_bounds__(256, batch_ctas_per_sm<T, EMAX, R2C>())
 k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restrict__ plans,
         c_t<T> const *const *__restrict__ tws, BatchBufs bufs, unsigned long long *work_counter, int *done,
-        long long total_tiles, int *status, int scaling, long long dep_budget, int pf_offset){
+        long long total_tiles, int *status, int scaling, long long dep_budget, int pf_offset, int nplans,
+        int tw_off){
     using C = c_t<T>;
+    using Opts = StageOpts<S5, TWT>;
     extern __shared__ __align__(16) unsigned char smraw[];
     C *sm = reinterpret_cast<C*>(smraw);
+    // the twiddle tables in shared memory (TWT): table of plan p at s_twoff[p]
+    __shared__ int s_twoff[TWT ? kBatchTwPlans : 1];
+    C *smtw = reinterpret_cast<C*>(smraw + (tw_off > 0 ? tw_off : 0));
+    if constexpr (TWT){
+        if (threadIdx.x == 0){
+            int o = 0;
+            for (int p = 0; p < nplans && p < kBatchTwPlans; p++){
+                s_twoff[p] = o;
+                for (int s = 1; s < plans[p].nstages; s++) o += plans[p].st[s].Ns * (plans[p].st[s].R - 1);
+            }
+        }
+        __syncthreads();
+        for (int p = 0; p < nplans && p < kBatchTwPlans; p++){
+            C const *g = tws[p];
+            C *d = smtw + s_twoff[p];
+            for (int s = 1; s < plans[p].nstages; s++){
+                Stage const S = plans[p].st[s];
+                int const R1 = S.R - 1;
+                for (int i = threadIdx.x; i < S.Ns * R1; i += blockDim.x){
+                    int k = i / R1, q1 = i - k * R1;
+                    d[S.tw + q1 * S.Ns + k] = __ldg(g + S.tw + i);
+                }
+            }
+        }
+    }
     // prefetch buffer after the exchange buffer (pf_offset < 0: no prefetch)
     unsigned char *pfbuf = smraw + (pf_offset > 0 ? pf_offset : 0);
     __shared__ long long s_tile, s_next;
@@ -235,7 +267,7 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
         PrefetchHook<decltype(prefetch_next)> const hook{prefetch_next, pf_offset > 0};
         long long lt = gt - U.tile0;
         Plan1D const &P = plans[U.plan];
-        C const *tw = tws[U.plan];
+        C const *tw = TWT ? static_cast<C const*>(smtw + s_twoff[U.plan]) : tws[U.plan];
         unsigned char const *srcb = reinterpret_cast<unsigned char const*>(U.src == 0 ? bufs.in : (U.src == 1 ? bufs.out : bufs.work));
         unsigned char *dstb = reinterpret_cast<unsigned char*>(U.dst == 1 ? bufs.out : bufs.work);
         double f = (scaling == 0) ? 1.0 : ((scaling == 1) ? U.scale : sqrt(U.scale));
@@ -254,15 +286,15 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 // boxes; the 16-value kernel keeps both paths, which measured
                 // faster for it, 1.41 against 1.48 ms)
                 if constexpr (EMAX == 8 || R2C)
-                    tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, std::integral_constant<bool, S5>{});
-                else if (U.cols) tile_r2c<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, std::integral_constant<bool, S5>{});
-                else tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, std::integral_constant<bool, S5>{});
+                    tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, Opts{});
+                else if (U.cols) tile_r2c<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, Opts{});
+                else tile_r2c<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfr, hook, Opts{});
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if constexpr (R2C) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
-                else if (U.cols) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
-                else tile_c2c<T, EMAX, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                if constexpr (R2C) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
+                else if (U.cols) tile_c2c<T, EMAX, true, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
+                else tile_c2c<T, EMAX, true, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
             }
         } else {
             if (R2C && U.kind == K_C2R){
@@ -270,15 +302,15 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
                 T *out = reinterpret_cast<T*>(dstb) + U.out_off;
                 // the c2r pass runs along x: line tiles (as for r2c above)
                 if constexpr (EMAX == 8 || R2C)
-                    tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
-                else if (U.cols) tile_c2r<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
-                else tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                    tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
+                else if (U.cols) tile_c2r<T, EMAX, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
+                else tile_c2r<T, EMAX, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
             } else {
                 C const *in = reinterpret_cast<C const*>(srcb) + U.in_off;
                 C *out = reinterpret_cast<C*>(dstb) + U.out_off;
-                if constexpr (R2C) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
-                else if (U.cols) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
-                else tile_c2c<T, EMAX, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, std::integral_constant<bool, S5>{});
+                if constexpr (R2C) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
+                else if (U.cols) tile_c2c<T, EMAX, false, true>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
+                else tile_c2c<T, EMAX, false, false>(P, U.Li, U.Lo, in, out, tw, U.G, U.tpb, sc, dsc, lt, sm, pfc, hook, Opts{});
             }
         }
         // publish completion of this tile
@@ -295,6 +327,8 @@ k_batch(BatchUnit const *__restrict__ units, int nunits, Plan1D const *__restric
 void const *batch_kernel_e16_any(int prec, bool fwd);
 void const *batch_kernel_e16_r2c(int prec, bool fwd);
 void const *batch_kernel_e16_r2c5(int prec, bool fwd);
+// the same (float) with the twiddle tables in shared memory
+void const *batch_kernel_e16_r2c5_tw(bool fwd);
 void const *batch_kernel_e8(int prec, bool fwd, bool r2c, bool s5);
 
 } // namespace gbfft

@@ -28,7 +28,19 @@ __device__ __forceinline__ int sm_index(int p, int loc, int TPB, int padn){
     return COLS ? (p * TPB + loc) : (loc * padn + p + (p >> 4));
 }
 
-template<int R, int EMAX, bool FWD, bool COLS, typename T, class LD, class ST>
+// Options of fft_run beyond the radix set: S5 (the radices of 5-smooth
+// lengths alone, as std::integral_constant<bool, S5>) and TWT (tw is the
+// twiddle table in shared memory with each stage's block transposed to
+// [q - 1][k]: a warp's threads, which hold consecutive k, read consecutive
+// entries).
+template<bool S5, bool TWT> struct StageOpts {
+    static constexpr bool value = S5;
+    static constexpr bool twt = TWT;
+};
+template<class X, class = void> struct opts_twt : std::false_type {};
+template<class X> struct opts_twt<X, std::void_t<decltype(X::twt)>> : std::integral_constant<bool, X::twt> {};
+
+template<int R, int EMAX, bool FWD, bool COLS, typename T, bool TWT = false, class LD, class ST>
 __device__ __forceinline__ void fft_stage(Stage const &S, int t, int Tt, bool active, bool first, bool to_global,
                                           c_t<T> *sm, int loc, int TPB, int padn,
                                           c_t<T> const *__restrict__ tw, Regs<T, EMAX> &r, LD &ld, ST &st){
@@ -61,10 +73,9 @@ __device__ __forceinline__ void fft_stage(Stage const &S, int t, int Tt, bool ac
             int hi = fdiv(j, S);
             int k = j - hi * S.Ns;
             if (!first && k != 0){
-                C const *w = tw + S.tw + k * (R - 1);
                 #pragma unroll
                 for (int q = 1; q < R; q++){
-                    C wq = __ldg(w + q - 1);
+                    C wq = TWT ? tw[S.tw + (q - 1) * S.Ns + k] : __ldg(tw + S.tw + k * (R - 1) + q - 1);
                     r.v[m * R + q] = FWD ? cmul(r.v[m * R + q], wq) : cmulc(r.v[m * R + q], wq);
                 }
             }
@@ -91,12 +102,14 @@ struct NoHook {
 // Runs the whole transform. If last_to_global is false the result is left in
 // shared memory (natural order) and the CTA is synchronised on return.
 // S5T: std::true_type compiles the radices of 5-smooth lengths alone (2, 3,
-// 4, 5, 8, 16; the caller guarantees the plan has no other): fewer registers
+// 4, 5, 8, 16; the caller guarantees the plan has no other): fewer registers;
+// or StageOpts<S5, TWT> (TWT: tw in shared memory, transposed per stage)
 template<int EMAX, bool FWD, bool COLS, typename T, class LD, class ST, class AF = NoHook, class S5T = std::false_type>
 __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t<T> *sm, int loc, int TPB, int padn,
                                         c_t<T> const *__restrict__ tw, bool last_to_global, LD &ld, ST &st,
                                         AF const &after_first = AF{}, S5T = S5T{}){
     constexpr bool S5 = S5T::value;
+    constexpr bool TWT = opts_twt<S5T>::value;
     constexpr bool HOOK = !std::is_same<AF, NoHook>::value;
     Regs<T, EMAX> r;
     if (P.nstages == 0){
@@ -116,15 +129,15 @@ __device__ __forceinline__ void fft_run(Plan1D const &P, int t, bool active, c_t
         bool first = (s == 0);
         bool tg = (s == P.nstages - 1) && last_to_global;
         switch (S.R){
-            case 16: if constexpr (EMAX >= 16) fft_stage<16, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 13: if constexpr (EMAX >= 13 && !S5) fft_stage<13, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 11: if constexpr (EMAX >= 11 && !S5) fft_stage<11, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 8: fft_stage<8, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 7: if constexpr (!S5) fft_stage<7, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 5: fft_stage<5, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 4: fft_stage<4, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            case 3: fft_stage<3, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
-            default: fft_stage<2, EMAX, FWD, COLS, T>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 16: if constexpr (EMAX >= 16) fft_stage<16, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 13: if constexpr (EMAX >= 13 && !S5) fft_stage<13, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 11: if constexpr (EMAX >= 11 && !S5) fft_stage<11, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 8: fft_stage<8, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 7: if constexpr (!S5) fft_stage<7, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 5: fft_stage<5, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 4: fft_stage<4, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            case 3: fft_stage<3, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
+            default: fft_stage<2, EMAX, FWD, COLS, T, TWT>(S, t, P.T, active, first, tg, sm, loc, TPB, padn, tw, r, ld, st); break;
         }
         if constexpr (HOOK){
             // a stage that ends in shared memory ends with a barrier; one that
