@@ -154,27 +154,10 @@ __host__ __device__ constexpr int pipe_nbuf(int N, int csize, bool cols, int kin
             2 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize > 114 * 1024 &&
             3 * pipe_tile_elems(N, pipe_tpb(N, csize, cols), kind) * csize <= 200 * 1024) ? 3 : 2;
 }
-// Twiddles of the pipelined plan of N (complex values): stage s > 0 holds
-// Ns * (R - 1) of them.
-__host__ __device__ constexpr int pipe_tw_count(int N, bool df = false){
-    int n = 0;
-    for (int s = 1; s < pipe_nstages(N, df); s++) n += pipe_ns(N, s, df) * (pipe_radix(N, s, df) - 1);
-    return n;
-}
-// Float line tiles of up to 1024 points read their twiddles from a copy of
-// the table in shared memory (after the exchange buffer), each stage's block
-// transposed to [q - 1][k]: the TT threads of a line hold consecutive k, so a
-// warp's read of twiddle q touches consecutive entries instead of one line of
-// L1 per k (a stride of R - 1 values in the Stockham table).  Column tiles
-// share k across the TPB columns of a warp and keep the global table.
-__host__ __device__ constexpr bool pipe_tws(int N, int csize, bool cols, bool df = false){
-    return !cols && !df && csize == 8 && N >= 32 && N <= 1024;
-}
 __host__ __device__ constexpr int pipe_smem(int N, int csize, bool cols, int kind, int loader, bool df = false){
     int tpb = pipe_tpb(N, csize, cols, df);
     return pipe_nbuf(N, csize, cols, kind, loader, df) * pipe_tile_elems(N, tpb, kind) * csize +
-           ((cols || df) ? 0 : tpb * pipe_padn(N) * csize) +
-           (pipe_tws(N, csize, cols, df) ? pipe_tw_count(N, df) * csize : 0);
+           ((cols || df) ? 0 : tpb * pipe_padn(N) * csize);
 }
 
 struct PipeParams {
@@ -210,20 +193,6 @@ __host__ __device__ constexpr int pipe_swz(int p){
 // exchange buffer).
 // SWZ: line tiles exchanged in the tile buffer itself (pitch N), element p of
 // a line at pipe_swz(p) (no padding, the bank spread of an XOR swizzle).
-// Copies the twiddles of stages S.. of the pipelined plan of N from the
-// Stockham table (stage block [k][q - 1]) to shared memory ([q - 1][k]).
-template<int N, int S, typename C>
-__device__ __forceinline__ void pipe_copy_twiddles(C *tws, C const *__restrict__ tw){
-    if constexpr (S < pipe_nstages(N)){
-        constexpr int R1 = pipe_radix(N, S) - 1, NS = pipe_ns(N, S), TWO = pipe_twoff(N, S);
-        for (int i = threadIdx.x; i < NS * R1; i += blockDim.x){
-            int k = i / R1, q1 = i - k * R1;
-            tws[TWO + q1 * NS + k] = __ldg(tw + TWO + i);
-        }
-        pipe_copy_twiddles<N, S + 1>(tws, tw);
-    }
-}
-
 template<typename T, int N, int TPB, int S, bool FWD, bool COLS, bool POST,
          int SEND = pipe_nstages(N, std::is_same<T, df>::value), bool SWZ = false, class LD, class ST>
 __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const *__restrict__ tw,
@@ -237,7 +206,6 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
         constexpr bool LAST = (S == NS - 1);
         constexpr bool TO_XCH = !LAST || POST;
         constexpr int LNS = cilog2(Ns), LNSR = cilog2(Ns * R);
-        constexpr bool TWS = pipe_tws(N, (int)sizeof(C), COLS, DFT);
         auto xi = [&](int p) -> int {
             if constexpr (COLS) return p * TPB + loc;
             else if constexpr (SWZ) return loc * N + pipe_swz(p);
@@ -260,12 +228,10 @@ __device__ __forceinline__ void pstage(int t, int loc, c_t<T> *xch, c_t<T> const
             int j = t + m * TT;
             int k = j & (Ns - 1);
             if constexpr (S > 0){
+                C const *w = tw + TWO + k * (R - 1);
                 #pragma unroll
                 for (int q = 1; q < R; q++){
-                    // TWS: tw is the transposed copy in shared memory
-                    C wq;
-                    if constexpr (TWS) wq = tw[TWO + (q - 1) * Ns + k];
-                    else wq = ldg_c(tw + TWO + k * (R - 1) + q - 1);
+                    C wq = ldg_c(w + q - 1);
                     v[m * R + q] = FWD ? cmul(v[m * R + q], wq) : cmulc(v[m * R + q], wq);
                 }
             }
@@ -337,10 +303,6 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
     extern __shared__ __align__(128) unsigned char smraw[];
     C *tiles = reinterpret_cast<C*>(smraw);
     C *xline = tiles + NBUF * TILE;  // line tiles: padded exchange buffer
-    // float line tiles of up to 1024 points: the twiddle table in shared
-    // memory after the exchange buffer (pipe_tws)
-    constexpr bool TWS = pipe_tws(N, (int)sizeof(C), COLS, DF);
-    C *twtab = xline + TPB * PADN;
     __shared__ __align__(8) uint64_t bar[NBUF];
     __shared__ unsigned s_emax[DF ? NT / 32 : 1];   // per-warp largest exponent of a tile (DF)
 
@@ -357,9 +319,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
         fence_mbar_init();
     }
     if (LOADER == LD_TENSOR && tid == 0) prefetch_tmap(&tmap);
-    if constexpr (TWS) pipe_copy_twiddles<N, 1>(twtab, reinterpret_cast<C const*>(P.tw));
     __syncthreads();
-    C const *twp = TWS ? static_cast<C const*>(twtab) : reinterpret_cast<C const*>(P.tw);
 
     // tile -> (block, first column) for column tiles, first line for line tiles
     auto tile_origin = [&](long long tile, long long &blk, long long &c0){
@@ -551,7 +511,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                 // the last stage writes the tile buffer (read only by stage 0),
                 // one thread stores the whole tile with a bulk copy
                 auto st = [&](int p, C x){ tb[loc * N + p] = P.do_scale ? cscale(x, sc) : x; };
-                pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, twp, v, ld0, st);
+                pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
                 fence_proxy_async_smem();
                 __syncthreads();
                 if (tid == 0){
@@ -561,7 +521,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                 }
             } else {
                 auto st = [&](int p, C x){ if (va) out[oa + p * oes] = P.do_scale ? cscale(x, sc) : x; };
-                pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, twp, v, ld0, st);
+                pstage<T, N, TPB, 0, FWD, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
             }
         } else if constexpr (KIND == PK_R2C_FWD || KIND == PK_R2R_FWD){
             auto ld0 = [&](int p) -> C {
@@ -578,7 +538,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                 return z;
             };
             auto st = [&](int, C){};
-            pstage<T, N, TPB, 0, true, COLS, true>(t, loc, xch, twp, v, ld0, st);
+            pstage<T, N, TPB, 0, true, COLS, true>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
             auto xi = [&](int p) -> int { return COLS ? (p * TPB + loc) : (loc * PADN + p + (p >> 4)); };
             if constexpr (KIND == PK_R2C_FWD){
                 C *out = reinterpret_cast<C*>(P.out);
@@ -666,7 +626,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                     stg[(2 * loc) * N + p] = x.x * s;
                     stg[(2 * loc + 1) * N + p] = x.y * s;
                 };
-                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, twp, v, ld0, st);
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
                 fence_proxy_async_smem();
                 __syncthreads();
                 if (tid == 0){
@@ -679,7 +639,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                     if (va) out[oa + p * oes] = x.x * s;
                     if (vb) out[obb + p * oes] = x.y * s;
                 };
-                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, twp, v, ld0, st);
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
             }
         } else {
             // PK_R2R_BWD: V[k] = 2 exp(i pi k / 2N) (Y[k] - i Y[N-k]), two lines per FFT
@@ -712,7 +672,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                     stg[(2 * loc) * N + m] = x.x * sg;
                     stg[(2 * loc + 1) * N + m] = x.y * sg;
                 };
-                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, twp, v, ld0, st);
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
                 fence_proxy_async_smem();
                 __syncthreads();
                 if (tid == 0){
@@ -727,7 +687,7 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
                     if (va) out[oa + m * oes] = x.x * sg;
                     if (vb) out[obb + m * oes] = x.y * sg;
                 };
-                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, twp, v, ld0, st);
+                pstage<T, N, TPB, 0, false, COLS, false>(t, loc, xch, reinterpret_cast<C const*>(P.tw), v, ld0, st);
             }
         }
         __syncthreads();
