@@ -394,10 +394,6 @@ __device__ __forceinline__ void pipe_body(PipeParams const &P, CUtensorMap const
         }
     };
 
-    // launched with programmatic serialization: the prologue above overlapped
-    // the previous pass; no global memory is touched before this wait
-    griddep_wait();
-    griddep_launch_dependents();
     uint32_t phase = 0;              // bit b: parity of the next wait on bar[b]
     long long tile = blockIdx.x;
     // the first NBUF - 1 tiles of this CTA

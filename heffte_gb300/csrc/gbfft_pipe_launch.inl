@@ -106,20 +106,8 @@ bool run_pipe(cudaStream_t s, PipeLaunch const &a){
         P.ntiles = (a.G + (long long)TPB * UNITS - 1) / ((long long)TPB * UNITS);
     }
     long long grid = std::min<long long>(P.ntiles, (long long)num_sms() * blocks_per_sm[dev & 63]);
-    // programmatic serialization: the kernel's prologue (barriers, tensor
-    // map prefetch) may run while the previous kernel of the stream drains;
-    // the kernel waits (griddepcontrol.wait) before its first global access
-    cudaLaunchConfig_t lc{};
-    lc.gridDim = dim3((unsigned)grid);
-    lc.blockDim = dim3(THREADS);
-    lc.dynamicSmemBytes = SMEM;
-    lc.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    lc.attrs = attr;
-    lc.numAttrs = 1;
-    check_cuda(cudaLaunchKernelEx(&lc, kern, P, tmap), "pipelined fft kernel launch");
+    kern<<<(unsigned)grid, THREADS, SMEM, s>>>(P, tmap);
+    check_cuda(cudaPeekAtLastError(), "pipelined fft kernel launch");
     return true;
 }
 

@@ -37,13 +37,6 @@ __device__ __forceinline__ void fence_proxy_async_smem(){
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Programmatic dependent launch: wait until the grids this one depends on
-// have completed and their memory is visible (a no-op for a grid launched
-// without the programmatic-serialization attribute), and let the grids that
-// depend on this one be scheduled before it ends (they wait in turn).
-__device__ __forceinline__ void griddep_wait(){ asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void griddep_launch_dependents(){ asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes){
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
