@@ -201,6 +201,10 @@ struct PipeRtParams {
 };
 void launch_pipe_rt(cudaStream_t s, int prec, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
                     size_t smem, int threads);
+// Float lengths with runtime-radix pipelined kernels compiled for their
+// default radix plan (one instantiation unit gbfft_pipe_rt_n<N>.cu each)
+#define GBFFT_RT_CT_LENGTHS(X) X(96) X(160) X(192) X(240) X(288) X(320) X(384) X(448) X(480) X(576) \
+                               X(640) X(720) X(768) X(960)
 // shared-memory bytes that the float kernel compiled for this plan adds to
 // the tiles (its twiddle table), 0 when no compiled kernel runs it
 size_t rt_ct_smem(Plan1D const &plan);

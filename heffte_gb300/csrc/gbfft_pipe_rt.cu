@@ -1,8 +1,8 @@
 // Instantiations and launch of the pipelined runtime-radix complex kernels
 // (gbfft_pipe_rt.cuh): float and double, forward and backward, line tiles
 // (1-D bulk copies) and column tiles (3-D tensor-map copies).  Float
-// transforms of the lengths in kRtCtLengths run the kernels compiled for
-// that length's plan (gbfft_pipe_rt_n*.cu) when the plan is the default one.
+// transforms of the lengths in GBFFT_RT_CT_LENGTHS run the kernels compiled
+// for that length's plan (gbfft_pipe_rt_n*.cu) when the plan is the default one.
 #include "gbfft_pipe_rt_launch.inl"
 
 namespace gbfft {
@@ -15,12 +15,9 @@ static size_t ct_smem(Plan1D const &plan){
 size_t rt_ct_smem(Plan1D const &plan){
     if (!rt_compiled_plans()) return 0;
     switch (plan.N){
-        case 320: return ct_smem<320>(plan);
-        case 384: return ct_smem<384>(plan);
-        case 448: return ct_smem<448>(plan);
-        case 480: return ct_smem<480>(plan);
-        case 640: return ct_smem<640>(plan);
-        case 768: return ct_smem<768>(plan);
+#define GBFFT_CASE(n) case n: return ct_smem<n>(plan);
+        GBFFT_RT_CT_LENGTHS(GBFFT_CASE)
+#undef GBFFT_CASE
         default: return 0;
     }
 }
@@ -28,12 +25,9 @@ size_t rt_ct_smem(Plan1D const &plan){
 static bool launch_ct(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap, size_t smem,
                       int threads){
     switch (P.plan.N){
-        case 320: return launch_pipe_rt_ct<320>(s, fwd, cols, P, tmap, smem, threads);
-        case 384: return launch_pipe_rt_ct<384>(s, fwd, cols, P, tmap, smem, threads);
-        case 448: return launch_pipe_rt_ct<448>(s, fwd, cols, P, tmap, smem, threads);
-        case 480: return launch_pipe_rt_ct<480>(s, fwd, cols, P, tmap, smem, threads);
-        case 640: return launch_pipe_rt_ct<640>(s, fwd, cols, P, tmap, smem, threads);
-        case 768: return launch_pipe_rt_ct<768>(s, fwd, cols, P, tmap, smem, threads);
+#define GBFFT_CASE(n) case n: return launch_pipe_rt_ct<n>(s, fwd, cols, P, tmap, smem, threads);
+        GBFFT_RT_CT_LENGTHS(GBFFT_CASE)
+#undef GBFFT_CASE
         default: return false;
     }
 }

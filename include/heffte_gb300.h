@@ -64,8 +64,9 @@ int heffte_gb300_version(void);
 
 /* No reference counterpart (tuning / diagnostics of this backend).
  * Kernel family used by all later calls of this process: 0 automatic
- * (pipelined power-of-two kernels where they apply; float lengths 320, 384,
- * 448, 480, 640 and 768 by kernels compiled for their radix plan), 1 generic
+ * (pipelined power-of-two kernels where they apply; float lengths 96, 160,
+ * 192, 240, 288, 320, 384, 448, 480, 576, 640, 720, 768 and 960 by kernels
+ * compiled for their radix plan), 1 generic
  * runtime-radix kernels only, 2 pipelined kernels wherever they apply, 3 as
  * 0 but every length that is not a power of two on the runtime radix plan. */
 int heffte_gb300_set_kernel_variant(int variant);

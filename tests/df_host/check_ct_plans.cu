@@ -32,7 +32,7 @@ int main(){
         }
         checked++;
     }
-    for (int N : {320, 384, 448, 480, 640, 768})
+    for (int N : {96, 160, 192, 240, 288, 320, 384, 448, 480, 576, 640, 720, 768, 960})
         if (!direct_length(N) || ct_plan(N, kEmax).nstages == 0){
             printf("FAIL: compiled length %d has no direct plan\n", N);
             fails++;

@@ -457,14 +457,14 @@ def test_power_of_two_kernel_variants(gb, variant, prec):
 
 @pytest.mark.parametrize("variant", [0, 3])
 def test_compiled_plan_lengths(gb, variant):
-    """The float lengths with kernels compiled for their radix plan (320, 384,
-    448, 480, 640, 768; variant 0) and the same lengths on the runtime radix
-    plan (variant 3): the length along each dimension (line tiles, column
-    tiles), partial tiles, three orders, forward and backward."""
+    """The float lengths with kernels compiled for their radix plan (96 ...
+    960; variant 0) and the same lengths on the runtime radix plan (variant
+    3): the length along each dimension (line tiles, column tiles), partial
+    tiles, three orders, forward and backward."""
     gb.set_kernel_variant(variant)
     try:
         rng = np.random.default_rng(70 + variant)
-        for N in (320, 384, 448, 480, 640, 768):
+        for N in (96, 160, 192, 240, 288, 320, 384, 448, 480, 576, 640, 720, 768, 960):
             for size in [(N, 13, 3), (5, N, 7), (3, 11, N)]:
                 n = int(np.prod(size))
                 x = rand_c(rng, n, 0)
