@@ -202,13 +202,16 @@ __device__ __forceinline__ void ct_copy_twiddles(C *tws, C const *__restrict__ t
     }
 }
 
-// float: compiled for two 512-thread CTAs per SM (64 registers, no spills).
+// float: compiled for two 512-thread CTAs per SM (64 registers, no spills);
+// the line tiles of a compiled plan (at most 256 threads, three CTAs per SM
+// by shared memory) for three 256-thread CTAs (85 registers).
 // NC: 0 for the runtime plan, else the length whose compile-time plan the
 // stages run (constant sizes, divisions and trip counts); TWS (NC != 0): its
 // twiddles copied to shared memory (the host adds their bytes), else read
 // from the global table.
 template<typename T, bool FWD, bool COLS, int LOADER, int NC, bool TWS>
-__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1)
+__global__ void __launch_bounds__((NC != 0 && !COLS) ? 256 : 512,
+                                  (NC != 0 && !COLS) ? 3 : (sizeof(T) == 4 ? 2 : 1))
 k_pipe_rt(PipeRtParams const __grid_constant__ P, const __grid_constant__ CUtensorMap tmap){
     using C = c_t<T>;
     constexpr int EMAX = kEmax;

@@ -52,6 +52,7 @@ template<>
 bool launch_pipe_rt_ct<GBFFT_RT_LEN>(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap,
                                      size_t smem, int threads){
     if (!ct_plan_matches<GBFFT_RT_LEN>(P.plan)) return false;
+    if (!cols && threads > 256) return false;   // compiled line kernels: 256 threads at most
     CUtensorMap const &m = *reinterpret_cast<CUtensorMap const*>(tmap);
     // P.ct: 1 twiddles in shared memory (counted in smem), 2 in global memory
     if (P.ct == 1) dispatch<float, GBFFT_RT_LEN, true>(s, fwd, cols, P, m, smem, threads);
