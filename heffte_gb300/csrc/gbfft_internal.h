@@ -213,6 +213,11 @@ size_t rt_ct_smem(Plan1D const &plan);
 template<int NC>
 bool launch_pipe_rt_ct(cudaStream_t s, bool fwd, bool cols, PipeRtParams const &P, void const *tmap, size_t smem,
                        int threads);
+// (explicit specializations, one per compiled length, defined in gbfft_pipe_rt_n<N>.cu)
+#define GBFFT_RT_CT_DECL(n) \
+    template<> bool launch_pipe_rt_ct<n>(cudaStream_t, bool, bool, PipeRtParams const &, void const *, size_t, int);
+GBFFT_RT_CT_LENGTHS(GBFFT_RT_CT_DECL)
+#undef GBFFT_RT_CT_DECL
 
 // one dispatcher per precision and kind group (c2c / r2c+c2r / r2r), kind = K_*
 bool launch_pipe_f32_c2c(cudaStream_t s, int kind, int N, bool cols, PipeLaunch const &a);
