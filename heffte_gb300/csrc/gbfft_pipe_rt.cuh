@@ -12,8 +12,14 @@
 //     in place in the tile.
 // With two tile slots the next tile is copied in while this one is
 // transformed; with one slot (float line tiles, and float column tiles when
-// two CTAs of two slots do not fit in an SM's shared memory) the two CTAs on
-// an SM overlap each other's copies.
+// no two-CTA form of two slots fits an SM's shared memory) the CTAs on an SM
+// overlap each other's copies.
+//
+// Float lengths of a fixed list (GBFFT_RT_CT_LENGTHS) also have kernels
+// compiled for their default plan (NC = N): the same pipeline with every
+// radix, butterfly count, division and trip count a constant, and the
+// twiddle table copied once per CTA into shared memory, transposed per stage
+// (TWS).  The host picks the slots, the tile width and TWS per launch.
 #pragma once
 #include <cuda.h>
 #include "gbfft_kernels.cuh"
