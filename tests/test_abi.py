@@ -117,6 +117,13 @@ def test_plan_option_setters_validate(gb):
         assert L.heffte_gb300_plan_set_knobs(p._h, *args) == 1
     assert L.heffte_gb300_plan_set_tensor_cores(None, 1) == 1
     assert p.size_inbox() == 64 * 32 * 16          # the plan survives rejected settings
+    # process-wide kernel family: 0 automatic, 1 generic, 2 pipelined, 3 automatic
+    # with runtime radix plans only; anything else is rejected and changes nothing
+    for v in (3, 2, 1, 0):
+        assert L.heffte_gb300_set_kernel_variant(v) == 0
+    for v in (-1, 4):
+        assert L.heffte_gb300_set_kernel_variant(v) == 1
+        assert b"variant" in L.heffte_gb300_last_error()
 
 
 def test_raw_abi_status_codes(gb):
