@@ -5,10 +5,12 @@
 // has the library's stages (radix, Ns, N / R, twiddle offset), threads per
 // transform and twiddle count, so a kernel compiled for any such length
 // would run that length's default plan.  Also checks that the lengths with
-// compiled kernels are among them.  No GPU call.
+// compiled kernels are among them, and that their per-stage transposed
+// twiddle copy is read back as the Stockham table.  No GPU call.
 #include "../../heffte_gb300/csrc/gbfft_pipe_rt.cuh"
 #include "../../heffte_gb300/csrc/gbfft_internal.h"
 #include <cstdio>
+#include <vector>
 
 using namespace gbfft;
 
@@ -37,6 +39,30 @@ int main(){
             printf("FAIL: compiled length %d has no direct plan\n", N);
             fails++;
         }
+    // the twiddle copy of the compiled kernels (ct_copy_twiddles: global
+    // entry TWO + i, i = k (R - 1) + q - 1, to TWO + (q - 1) Ns + k) read back
+    // where the stages read it (fft_stage_ct with TWS) gives the Stockham
+    // table's entry of butterfly column k and twiddle q, for every stage
+    for (int N : {96, 160, 192, 240, 288, 320, 384, 448, 480, 576, 640, 720, 768, 960}){
+        CtPlan const c = ct_plan(N, kEmax);
+        int const n = ct_twiddles(N, kEmax);
+        std::vector<int> g(n), d(n, -1);
+        for (int i = 0; i < n; i++) g[i] = i;
+        for (int s = 1; s < c.nstages; s++){
+            int const R1 = c.R[s] - 1;
+            for (int i = 0; i < c.Ns[s] * R1; i++){
+                int k = i / R1, q1 = i - k * R1;
+                d[c.tw[s] + q1 * c.Ns[s] + k] = g[c.tw[s] + i];
+            }
+        }
+        for (int s = 1; s < c.nstages; s++)
+            for (int k = 0; k < c.Ns[s]; k++)
+                for (int q = 1; q < c.R[s]; q++)
+                    if (d[c.tw[s] + (q - 1) * c.Ns[s] + k] != c.tw[s] + k * (c.R[s] - 1) + q - 1){
+                        printf("FAIL: N=%d stage %d k=%d q=%d: transposed twiddle\n", N, s, k, q);
+                        fails++;
+                    }
+    }
     printf("%d lengths checked\n", checked);
     if (fails == 0) printf("compile-time plans ok\n");
     return fails ? 1 : 0;
